@@ -1,0 +1,134 @@
+"""In-tree build of the engine (CUDA, sm_103a), the C command-line tool and the oracle.
+
+Everything is compiled with plain nvcc / gcc command lines, in parallel, into ``_build/``
+directories next to the sources (git-ignored).  No cmake, no pip install: the library that the
+tests and the bench load is the one built here, in the tree.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+INCLUDE = ROOT / "include"
+BUILD = PKG / "_build"
+ORACLE = ROOT / "oracle"
+ORACLE_BUILD = ORACLE / "_build"
+
+ARCH = os.environ.get("AST_CUDA_ARCH", "sm_103a")
+GENCODE = [f"-gencode=arch=compute_{ARCH[3:]},code={ARCH}"]
+CU_SOURCES = ["csrc/engine.cu", "csrc/fit.cu"]
+C_SOURCES = ["host/tables.c", "host/read_data.c", "host/errors.c"]
+CLI_SOURCES = ["host/asteroid.c", "host/misc.c"]
+
+
+def _nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and Path(cand).exists():
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _cuda_lib_dir() -> Path:
+    nvcc = Path(_nvcc()).resolve()
+    for cand in (nvcc.parent.parent / "lib64", nvcc.parent.parent / "targets" / "sbsa-linux" / "lib",
+                 nvcc.parent.parent / "targets" / "x86_64-linux" / "lib"):
+        if (cand / "libcudart.so").exists() or (cand / "libcudart_static.a").exists():
+            return cand
+    return nvcc.parent.parent / "lib64"
+
+
+def _run(cmd: list[str]) -> None:
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"build step failed ({r.returncode}): {' '.join(cmd)}\n{r.stdout}")
+    if os.environ.get("AST_BUILD_VERBOSE") and r.stdout.strip():
+        print(r.stdout, file=sys.stderr)
+
+
+def _stale(target: Path, deps: list[Path]) -> bool:
+    if not target.exists():
+        return True
+    t = target.stat().st_mtime
+    return any(d.stat().st_mtime > t for d in deps)
+
+
+def _headers() -> list[Path]:
+    return sorted(list(PKG.glob("csrc/*.cuh")) + list(PKG.glob("host/*.h")) + list(INCLUDE.glob("*.h")))
+
+
+def build_engine(force: bool = False, ptxas_verbose: bool = False) -> Path:
+    """Compile libasteroid_gb300.so (CUDA engine + C host code) and the asteroid CLI."""
+    BUILD.mkdir(exist_ok=True)
+    nvcc = _nvcc()
+    hdrs = _headers()
+    objs: list[Path] = []
+    jobs = []
+    for src in CU_SOURCES:
+        s = PKG / src
+        o = BUILD / (s.stem + ".o")
+        objs.append(o)
+        if force or _stale(o, [s] + hdrs):
+            cmd = [nvcc, *GENCODE, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
+                   f"-I{INCLUDE}", f"-I{PKG / 'host'}", "-c", str(s), "-o", str(o)]
+            if ptxas_verbose:
+                cmd.insert(1, "-Xptxas=-v")
+            jobs.append(cmd)
+    for src in C_SOURCES:
+        s = PKG / src
+        o = BUILD / (s.stem + ".o")
+        objs.append(o)
+        if force or _stale(o, [s] + hdrs):
+            jobs.append(["gcc", "-O2", "-fPIC", "-std=c11", "-Wall", f"-I{INCLUDE}", f"-I{PKG / 'host'}",
+                         "-c", str(s), "-o", str(o)])
+    with ThreadPoolExecutor(max_workers=max(4, os.cpu_count() or 4)) as ex:
+        list(ex.map(_run, jobs))
+    lib = BUILD / "libasteroid_gb300.so"
+    if force or jobs or not lib.exists():
+        _run([nvcc, *GENCODE, "-shared", "-o", str(lib), *map(str, objs), "-lcudart"])
+    cli = BUILD / "asteroid"
+    cli_src = [PKG / s for s in CLI_SOURCES if (PKG / s).exists()]
+    if cli_src and (force or _stale(cli, cli_src + hdrs + [lib])):
+        _run(["gcc", "-O2", "-std=c11", "-Wall", f"-I{INCLUDE}", f"-I{PKG / 'host'}", *map(str, cli_src),
+              "-o", str(cli), f"-L{BUILD}", "-lasteroid_gb300", f"-Wl,-rpath,{BUILD}", "-lm"])
+    return lib
+
+
+def build_oracle(force: bool = False) -> Path:
+    """Compile the CPU oracle (test infrastructure) with OpenMP and without fused multiply-adds."""
+    ORACLE_BUILD.mkdir(exist_ok=True)
+    src = ORACLE / "chi2_oracle.c"
+    deps = [src] + sorted(ORACLE.glob("*.h")) + [INCLUDE / "asteroid_gb300.h"]
+    lib = ORACLE_BUILD / "liboracle.so"
+    if force or _stale(lib, deps):
+        _run(["gcc", "-O2", "-fPIC", "-shared", "-std=c11", "-ffp-contract=off", "-fopenmp", f"-I{INCLUDE}",
+              str(src), "-o", str(lib), "-lm"])
+    return lib
+
+
+def build_reference_oracle() -> None:
+    """Where the reference checkout is present, build its own chi^2 code (oracle/_ref)."""
+    script = ORACLE / "build_ref.sh"
+    ref = Path(os.environ.get("AST_REFERENCE_DIR", "/root/reference"))
+    if script.exists() and (ref / "cuda.c").exists():
+        have = list((ORACLE / "_ref").glob("libref_*.so")) if (ORACLE / "_ref").exists() else []
+        if not have:
+            _run(["bash", str(script)])
+
+
+def build(force: bool = False) -> None:
+    with ThreadPoolExecutor(max_workers=2) as ex:
+        f1 = ex.submit(build_engine, force)
+        f2 = ex.submit(build_oracle, force)
+        f1.result()
+        f2.result()
+
+
+if __name__ == "__main__":
+    build(force="--force" in sys.argv)
+    print("built", BUILD / "libasteroid_gb300.so")

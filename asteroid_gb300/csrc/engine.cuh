@@ -1,0 +1,88 @@
+// engine.cuh -- the context object behind the C ABI and the helpers the kernels share.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "asteroid_gb300.h"
+#include "model.cuh"
+
+extern "C" int ast_set_error(int code, const char* fmt, ...);
+
+#define AST_CUDA(call)                                                                        \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            return ast_set_error(AST_E_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, #call,       \
+                                 cudaGetErrorString(e_));                                     \
+    } while (0)
+
+namespace ast {
+
+// Device error word: kernels record a wait that ran out of iterations here instead of
+// trapping, so the context stays usable and the host returns AST_E_TIMEOUT.
+enum : int32_t { kErrNone = 0, kErrStageTimeout = 1 };
+
+struct FitBuffers {
+    int64_t slots = 0, slots_pad = 0, chains = 0, groups = 0;
+    int32_t n_params = 0, n_filters = 0, cf_bytes = 0;
+    void* x = nullptr;        // CF [(N+1)*N][S]
+    void* f = nullptr;        // CF [N+1][S]
+    uint8_t* ind = nullptr;   // [N+1][S]
+    void* x0 = nullptr;       // CF [N][S]
+    void* xr = nullptr;       // CF [N][S]
+    void* fr = nullptr;       // CF [S]
+    int32_t* st = nullptr;    // [S] phase | j << 8 | bad << 16
+    int32_t* it = nullptr;    // [S] simplex iterations l
+    int32_t* ev = nullptr;    // [S] evaluations of the current chain-stage
+    int64_t* chain = nullptr; // [S] chain on the slot, -1 if none
+    double* dv = nullptr;     // [NF][S] last delta_V of the slot's chain
+    double* chain_f = nullptr;  // [C]
+    void* chain_x = nullptr;    // CF [C][N] best vertex
+    double* chain_dv = nullptr; // [C][NF]
+    void* group_x = nullptr;    // CF [G][N] next stage start
+    double* out_f = nullptr;    // [G]
+    double* out_p = nullptr;    // [G][N]
+    double* out_dv = nullptr;   // [G][NF]
+    unsigned long long* ctr = nullptr;  // [0] next chain, [1] finished chains, [2] evals, [3] fits, [4] err
+    size_t bytes = 0;
+    void* base = nullptr;
+};
+
+struct FitRun {
+    bool active = false;
+    ast_fit_cfg cfg{};
+    int32_t stage = 0;
+    int32_t reopt = 0;          // reopt of the current stage
+    int64_t n_evals = 0, n_fits = 0;
+    double kernel_ms = 0;
+    int tpb = 256, ctas = 0;
+    size_t smem = 0;
+    bool stage_obs_in_smem = true;
+};
+
+}  // namespace ast
+
+struct ast_ctx {
+    int device = 0;
+    int sm_count = 0;
+    size_t smem_optin = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    ast_model model{};
+    ast::DevModel dm{};
+    int32_t n_data = 0, n_filters = 0;
+    ast::ObsLayout layout{};
+    void* d_obs = nullptr;
+    // evaluation scratch
+    double* d_params = nullptr;
+    double* d_chi2 = nullptr;
+    double* d_dv = nullptr;
+    int64_t eval_cap = 0;
+    // fit
+    ast::FitBuffers fb;
+    ast::FitRun run;
+};
+
+namespace ast {
+int build_dev_model(const ast_model* m, const ast_obs_set* obs, DevModel* dm);
+int set_device(int device);
+}  // namespace ast

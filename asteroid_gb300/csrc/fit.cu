@@ -1,0 +1,693 @@
+// fit.cu -- the downhill-simplex / random-search driver as a persistent device loop.
+//
+// The reference runs one Nelder-Mead chain per thread of chi2_gpu<<<N_BLOCKS, BSIZE>>>
+// (cuda.c:1326-1833), keeps each simplex in local memory (255 registers plus spills on
+// sm_103a), and lets a thread whose chain converged idle until its block finishes.  Here:
+//
+//   * every thread is a persistent "slot" that pulls chains from a device-wide pool with an
+//     atomic counter, so a chain that converges early is replaced at once;
+//   * the simplex of each slot lives in HBM as structure-of-arrays indexed [k][slot], so a
+//     warp's 32 slots touch 32 consecutive words (coalesced), and registers stay with chi^2;
+//   * the chain is a state machine (INIT j, REFLECT, EXPAND, CONTRACT, SHRINK j) in which every
+//     loop iteration performs exactly one chi^2 evaluation: all lanes of a warp evaluate
+//     together, and the RK4 trip counts are the same for every lane (they depend on the
+//     observation times only), so the hot loop does not diverge;
+//   * a launch runs until every slot has spent its evaluation budget or the pool is empty and
+//     saves its state, so a fit can be advanced in bounded steps (bench, serving);
+//   * stages (-Nstages) are separate pools; between them group_best_kernel takes each group's
+//     best chain (the reference's per-block argmin and hand-off, cuda.c:1769-1805).
+// The chain semantics (random start, initial simplex, sort with ties to the last index,
+// centroid over all N+1 vertices, reflect/expand/contract/shrink tests, failure rules,
+// iteration cap) are those of cuda.c:1424-1742; the restatement in oracle/nm_oracle_body.h
+// follows the same steps on the CPU.
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <string.h>
+#include <vector>
+
+#include "asteroid_gb300.h"
+#include "engine.cuh"
+#include "mixed.cuh"
+#include "model.cuh"
+#include "philox.cuh"
+#include "staging.cuh"
+
+size_t ast_obs_smem(const ast_ctx* c);
+
+namespace ast {
+
+enum : int32_t { PH_INIT = 0, PH_REFLECT = 1, PH_EXPAND = 2, PH_CONTRACT = 3, PH_SHRINK = 4 };
+
+template <class CF>
+struct FitView {
+    CF* x;
+    CF* f;
+    uint8_t* ind;
+    CF* x0;
+    CF* xr;
+    CF* fr;
+    int32_t* st;
+    int32_t* it;
+    int32_t* ev;
+    int64_t* chain;
+    double* dv;
+    double* chain_f;
+    CF* chain_x;
+    double* chain_dv;
+    CF* group_x;
+    unsigned long long* ctr;
+    int64_t S;          // slot stride (padded slot count)
+    int64_t n_slots;
+    int64_t n_chains;
+    int32_t group_size;
+    int32_t stage;
+    int32_t reopt;
+    int32_t last_stage;
+    uint64_t seed;
+    int64_t evals_cap;
+    int32_t steps_cap;
+};
+
+template <class CF>
+struct NMConst;
+template <>
+struct NMConst<double> {
+    static constexpr double DX_INI = 0.001, D2X_INI = -1.2, DX_RAND = 0.0001;
+    __device__ static double size2_min() { return 1e-10 * 1e-10; }
+};
+template <>
+struct NMConst<float> {
+    static constexpr float DX_INI = 0.001f, D2X_INI = -1.2f, DX_RAND = 0.0001f;
+    __device__ static float size2_min() { return 1e-5f * 1e-5f; }
+};
+__device__ __forceinline__ double cf_exp(double v) { return exp(v); }
+__device__ __forceinline__ float cf_exp(float v) { return expf(v); }
+
+__device__ __forceinline__ bool hard_side(int per, int LAM, bool left)
+{
+    if (per == AST_HARD_BOTH) return true;
+    if (left && per == AST_HARD_LEFT) return true;
+    if (!left && per == AST_HARD_RIGHT) return true;
+    return LAM == 0 && per == AST_PERIODIC_LAM;
+}
+
+#define XV(v, i) V.x[((int64_t)(v) * N + (i)) * S + s]
+#define FV(v) V.f[(int64_t)(v) * S + s]
+#define IND(v) V.ind[(int64_t)(v) * S + s]
+#define X0V(i) V.x0[(int64_t)(i) * S + s]
+#define XRV(i) V.xr[(int64_t)(i) * S + s]
+
+// Random start point and initial simplex of chain c (cuda.c:1459-1545).
+template <class CF>
+__device__ void start_chain(const DevModel& M, const FitView<CF>& V, int64_t s, int64_t c)
+{
+    const int N = M.n_params;
+    const int64_t S = V.S;
+    const ast_type_ids& T = M.t;
+    const int reopt = V.reopt;
+    const double SMALL = 1e-8;
+    const CF DX_INI = NMConst<CF>::DX_INI, D2X_INI = NMConst<CF>::D2X_INI, DX_RAND = NMConst<CF>::DX_RAND;
+    CF x0[AST_MAX_PARAMS];
+    const int64_t g = c / V.group_size;
+    for (int i = 0; i < N; i++) x0[i] = reopt ? V.group_x[g * N + i] : (CF)0;
+    uint32_t k = 0;
+    int LAM = 0;
+    for (int i = 0; i < N; i++) {
+        const float r = uniform01(V.seed, (uint64_t)c, (uint32_t)V.stage, k++);
+        const int pt = M.ptype[i], per = M.periodic[i];
+        if ((M.flags & AST_BC) && !reopt) {
+            if (pt == T.c) { x0[i] = x0[M.idx[T.c_tumb]]; continue; }
+            if (pt == T.b) { x0[i] = x0[M.idx[T.b_tumb]]; continue; }
+        }
+        if (!reopt || M.frozen[i] == -1) {
+            x0[i] = (CF)(DX_INI + SMALL + r * (1.0 - 2 * (SMALL + DX_INI)));
+        } else {
+            CF xmin = x0[i] - DX_RAND;
+            CF xmax = x0[i] + DX_RAND;
+            if (xmin < SMALL && hard_side(per, LAM, true)) xmin = (CF)SMALL;
+            if (xmax > 1.0 - SMALL && hard_side(per, LAM, false)) xmax = (CF)(1.0 - SMALL);
+            x0[i] = xmin + r * (xmax - xmin);
+        }
+        if (pt == T.Es) LAM = x0[i] >= 0.5;
+    }
+    for (int i = 0; i < N; i++) XV(0, i) = x0[i];
+    for (int j = 1; j <= N; j++) {
+        for (int i = 0; i < N; i++) {
+            CF xv = x0[i];
+            if (i == j - 1) {
+                const int per = M.periodic[i];
+                const float d2x = uniform01(V.seed, (uint64_t)c, (uint32_t)V.stage, k++);
+                CF dx = DX_INI * cf_exp(D2X_INI * d2x);
+                if (uniform01(V.seed, (uint64_t)c, (uint32_t)V.stage, k++) < 0.5) {
+                    dx = -dx;
+                    if (x0[i] + dx < SMALL && hard_side(per, LAM, true)) dx = -dx;
+                } else {
+                    if (x0[i] + dx > 1.0 - SMALL && hard_side(per, LAM, false)) dx = -dx;
+                }
+                xv = x0[i] + dx;
+            }
+            XV(j, i) = xv;
+        }
+    }
+    for (int j = 0; j <= N; j++) IND(j) = (uint8_t)j;
+}
+
+template <class CF, int PREC>
+__device__ __forceinline__ CF eval_point(const DevModel& M, const ObsView& o, const double* params, CF* dv)
+{
+    if (PREC == AST_PREC_FP64) return chi2_fp64<CF>(M, o, params, dv);
+    return chi2_mixed<CF>(M, o, params, dv);
+}
+
+template <class CF, int PREC>
+__global__ void __launch_bounds__(256) fit_kernel(DevModel M, const void* g_obs, ObsLayout L, int use_smem,
+                                                  FitView<CF> V, int64_t budget)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ uint64_t bar;
+    const bool staged = use_smem ? bulk_stage(smem, g_obs, (uint32_t)L.bytes, &bar, &V.ctr[4]) : false;
+    const ObsView o = L.view(staged ? (const void*)smem : g_obs, M.n_data);
+    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int N = M.n_params, NF = M.n_filters;
+    const int64_t S = V.S;
+    if (s < V.n_slots) {
+        int64_t chain = V.chain[s];
+        int32_t st = V.st[s], l = V.it[s], ev = V.ev[s];
+        CF dvl[AST_MAX_FILTERS];
+        for (int m = 0; m < NF; m++) dvl[m] = (CF)V.dv[(int64_t)m * S + s];
+        const CF HUGEV = (CF)kHuge;
+        const CF size2_min = NMConst<CF>::size2_min();
+        int64_t used = 0;
+        unsigned long long n_ev = 0, n_fit = 0;
+        while (true) {
+            if (chain < 0) {
+                const unsigned long long c = atomicAdd(&V.ctr[0], 1ull);
+                if (c >= (unsigned long long)V.n_chains) break;
+                chain = (int64_t)c;
+                start_chain<CF>(M, V, s, chain);
+                st = PH_INIT;
+                l = 0;
+                ev = 0;
+                for (int m = 0; m < NF; m++) dvl[m] = V.stage > 0 ? (CF)V.chain_dv[chain * NF + m] : (CF)0;
+            }
+            const int phase = st & 0xff;
+            int j = (st >> 8) & 0xff;
+            int bad = (st >> 16) & 1;
+            CF p[AST_MAX_PARAMS];
+            if (phase == PH_INIT) {
+                for (int i = 0; i < N; i++) p[i] = XV(j, i);
+            } else if (phase == PH_REFLECT || phase == PH_CONTRACT) {
+                for (int i = 0; i < N; i++) p[i] = XRV(i);
+            } else if (phase == PH_EXPAND) {
+                for (int i = 0; i < N; i++) {
+                    const CF c0 = X0V(i);
+                    p[i] = (M.frozen[i] != 1) ? c0 + (CF)2.0 * (XRV(i) - c0) : c0;
+                }
+            } else {
+                const int v = IND(j);
+                for (int i = 0; i < N; i++) p[i] = XV(v, i);
+            }
+            // One evaluation: x -> params (hard limits), then chi^2.
+            double params[AST_MAX_PARAMS];
+            const int rej = x2params<CF>(M, V.reopt, p, params);
+            CF fv = HUGEV;
+            if (!rej) {
+                fv = eval_point<CF, PREC>(M, o, params, dvl);
+                ev++;
+                n_ev++;
+            }
+            used++;
+            bool iter_top = false, finish = false, failed = false;
+            if (phase == PH_INIT) {
+                if (rej) {
+                    finish = failed = true;
+                } else {
+                    FV(j) = fv;
+                    j++;
+                    if (j > N) iter_top = true;
+                    else st = PH_INIT | (j << 8);
+                }
+            } else if (phase == PH_REFLECT) {
+                const CF f_r = rej ? HUGEV : fv;
+                const int b = IND(0), sw = IND(N - 1), w = IND(N);
+                if (f_r >= FV(b) && f_r < FV(sw)) {
+                    for (int i = 0; i < N; i++) XV(w, i) = p[i];
+                    FV(w) = f_r;
+                    iter_top = true;
+                } else if (f_r < FV(b)) {
+                    V.fr[s] = f_r;
+                    st = PH_EXPAND;
+                } else {
+                    for (int i = 0; i < N; i++) {
+                        const CF c0 = X0V(i);
+                        XRV(i) = (M.frozen[i] != 1) ? c0 + (CF)0.5 * (XV(w, i) - c0) : c0;
+                    }
+                    st = PH_CONTRACT;
+                }
+            } else if (phase == PH_EXPAND) {
+                const CF f_e = rej ? HUGEV : fv;
+                const CF f_r = V.fr[s];
+                const int w = IND(N);
+                if (f_e < f_r) {
+                    for (int i = 0; i < N; i++) XV(w, i) = p[i];
+                    FV(w) = f_e;
+                } else {
+                    for (int i = 0; i < N; i++) XV(w, i) = XRV(i);
+                    FV(w) = f_r;
+                }
+                iter_top = true;
+            } else if (phase == PH_CONTRACT) {
+                const CF f_c = rej ? HUGEV : fv;
+                const int w = IND(N);
+                if (f_c < FV(w)) {
+                    for (int i = 0; i < N; i++) XV(w, i) = p[i];
+                    FV(w) = f_c;
+                    iter_top = true;
+                } else {
+                    // Shrink every vertex but the best towards it (cuda.c:1716-1727).
+                    const int b = IND(0), v = IND(1);
+                    for (int i = 0; i < N; i++)
+                        if (M.frozen[i] != 1) XV(v, i) = XV(b, i) + (CF)0.5 * (XV(v, i) - XV(b, i));
+                    st = PH_SHRINK | (1 << 8);
+                }
+            } else {  // PH_SHRINK
+                if (rej) bad = 1;
+                else FV(IND(j)) = fv;
+                j++;
+                if (j <= N) {
+                    const int b = IND(0), v = IND(j);
+                    for (int i = 0; i < N; i++)
+                        if (M.frozen[i] != 1) XV(v, i) = XV(b, i) + (CF)0.5 * (XV(v, i) - XV(b, i));
+                    st = PH_SHRINK | (j << 8) | (bad << 16);
+                } else if (bad) {
+                    finish = failed = true;
+                } else {
+                    iter_top = true;
+                }
+            }
+            if (iter_top) {
+                l++;
+                // Selection sort, ties to the last index; an all-NaN simplex keeps ind[0] = 0
+                // with f = 1e30 (cuda.c:1575-1601).
+                uint32_t taken = 0;
+                for (int jj = 0; jj <= N; jj++) {
+                    CF fmin = HUGEV;
+                    int jmin = -1;
+                    for (int j2 = 0; j2 <= N; j2++) {
+                        const CF fj = FV(j2);
+                        if (!(taken >> j2 & 1u) && fj <= fmin) { fmin = fj; jmin = j2; }
+                    }
+                    if (jmin < 0) {
+                        IND(0) = 0;
+                        FV(0) = HUGEV;
+                        break;
+                    }
+                    IND(jj) = (uint8_t)jmin;
+                    taken |= 1u << jmin;
+                }
+                // Centroid of all N+1 vertices and the size test (cuda.c:1604-1632).
+                CF size2 = 0;
+                for (int i = 0; i < N; i++) {
+                    CF sum = 0;
+                    for (int v = 0; v <= N; v++) sum = sum + XV(v, i);
+                    X0V(i) = sum / (CF)(N + 1);
+                }
+                for (int v = 0; v <= N; v++) {
+                    CF sum = 0;
+                    for (int i = 0; i < N; i++) {
+                        const CF dx = XV(v, i) - X0V(i);
+                        sum = sum + dx * dx;
+                    }
+                    size2 = size2 + sum;
+                }
+                size2 = size2 / (CF)N;
+                if (size2 < size2_min || l > V.steps_cap || (V.evals_cap > 0 && ev >= V.evals_cap)) {
+                    finish = true;
+                } else {
+                    const int w = IND(N);
+                    for (int i = 0; i < N; i++) {
+                        const CF c0 = X0V(i);
+                        XRV(i) = (M.frozen[i] != 1) ? c0 + (CF)1.0 * (c0 - XV(w, i)) : c0;
+                    }
+                    st = PH_REFLECT;
+                }
+            }
+            if (finish) {
+                const int b = failed ? 0 : IND(0);
+                V.chain_f[chain] = failed ? kHuge : (double)FV(b);
+                for (int i = 0; i < N; i++) V.chain_x[chain * N + i] = XV(b, i);
+                for (int m = 0; m < NF; m++) V.chain_dv[chain * NF + m] = (double)dvl[m];
+                atomicAdd(&V.ctr[1], 1ull);
+                n_fit += V.last_stage ? 1 : 0;
+                chain = -1;
+            }
+            if (used >= budget) break;
+        }
+        V.chain[s] = chain;
+        V.st[s] = st;
+        V.it[s] = l;
+        V.ev[s] = ev;
+        for (int m = 0; m < NF; m++) V.dv[(int64_t)m * S + s] = (double)dvl[m];
+        if (n_ev) atomicAdd(&V.ctr[2], n_ev);
+        if (n_fit) atomicAdd(&V.ctr[3], n_fit);
+    }
+    bulk_drain(&bar, staged || !use_smem);
+}
+#undef XV
+#undef FV
+#undef IND
+#undef X0V
+#undef XRV
+
+// Per-group argmin over the chains' results (lowest chi^2, lowest chain on ties, as the serial
+// loop of cuda.c:1770-1782) and the stage hand-off or the final output (cuda.c:1785-1823).
+template <class CF>
+__global__ void group_best_kernel(DevModel M, FitView<CF> V, double* out_f, double* out_p, double* out_dv)
+{
+    const int64_t g = blockIdx.x;
+    const int N = M.n_params, NF = M.n_filters;
+    double best = kHuge;
+    int64_t bi = INT64_MAX;
+    for (int64_t c = g * V.group_size + threadIdx.x; c < (g + 1) * V.group_size; c += blockDim.x) {
+        const double f = V.chain_f[c];
+        if (f < best || (f == best && c < bi)) { best = f; bi = c; }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        const double of = __shfl_down_sync(0xffffffffu, best, off);
+        const long long oi = __shfl_down_sync(0xffffffffu, (long long)bi, off);
+        if (of < best || (of == best && oi < bi)) { best = of; bi = oi; }
+    }
+    __shared__ double sf[32];
+    __shared__ long long si[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) { sf[warp] = best; si[warp] = bi; }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    for (int w = 1; w < (int)(blockDim.x + 31) / 32; w++)
+        if (sf[w] < best || (sf[w] == best && si[w] < bi)) { best = sf[w]; bi = si[w]; }
+    // Strictly below 1e30, else the group's first chain (the reference's thread_min = 0).
+    const int64_t cb = (best < kHuge) ? bi : g * V.group_size;
+    CF xb[AST_MAX_PARAMS];
+    for (int i = 0; i < N; i++) xb[i] = V.chain_x[cb * N + i];
+    if (!V.last_stage) {
+        if ((M.flags & AST_P_PSI) && V.reopt == 0) {
+            // P_PSI hand-off: x of L changes meaning from 1/Ppsi to L (cuda.c:1788-1799).
+            double p[AST_MAX_PARAMS];
+            x2params<CF>(M, 0, xb, p);
+            params2x<CF>(M, p, xb);
+        }
+        for (int i = 0; i < N; i++) V.group_x[g * N + i] = xb[i];
+    } else {
+        out_f[g] = best < kHuge ? best : kHuge;
+        double p[AST_MAX_PARAMS];
+        for (int i = 0; i < N; i++) p[i] = 0;
+        if (best < kHuge) x2params<CF>(M, V.reopt, xb, p);
+        for (int i = 0; i < N; i++) out_p[g * N + i] = p[i];
+        for (int m = 0; m < NF; m++) out_dv[g * NF + m] = best < kHuge ? V.chain_dv[cb * NF + m] : 0.0;
+    }
+}
+
+__global__ void reset_slots_kernel(int64_t* chain, int32_t* st, int32_t* it, int32_t* ev, double* dv, int64_t S, int NF)
+{
+    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    chain[s] = -1;
+    st[s] = 0;
+    it[s] = 0;
+    ev[s] = 0;
+    for (int m = 0; m < NF; m++) dv[(int64_t)m * S + s] = 0.0;
+}
+
+}  // namespace ast
+
+using namespace ast;
+
+template <class CF>
+static FitView<CF> make_view(ast_ctx* c)
+{
+    FitBuffers& b = c->fb;
+    FitView<CF> V;
+    V.x = (CF*)b.x; V.f = (CF*)b.f; V.ind = b.ind; V.x0 = (CF*)b.x0; V.xr = (CF*)b.xr; V.fr = (CF*)b.fr;
+    V.st = b.st; V.it = b.it; V.ev = b.ev; V.chain = b.chain; V.dv = b.dv;
+    V.chain_f = b.chain_f; V.chain_x = (CF*)b.chain_x; V.chain_dv = b.chain_dv; V.group_x = (CF*)b.group_x;
+    V.ctr = b.ctr;
+    V.S = b.slots_pad;
+    V.n_slots = b.slots;
+    V.n_chains = c->run.cfg.n_chains;
+    V.group_size = c->run.cfg.group_size;
+    V.stage = c->run.stage;
+    V.reopt = c->run.reopt;
+    V.last_stage = c->run.stage == c->run.cfg.n_stages - 1;
+    V.seed = c->run.cfg.seed;
+    V.evals_cap = c->run.cfg.evals_cap;
+    V.steps_cap = c->run.cfg.steps_cap > 0 ? c->run.cfg.steps_cap : 5000;
+    return V;
+}
+
+extern "C" void ast_fit_free(ast_ctx* c)
+{
+    if (c && c->fb.base) cudaFree(c->fb.base);
+    if (c) c->fb = FitBuffers();
+}
+
+static int fit_alloc(ast_ctx* c, int64_t slots, int64_t chains, int64_t groups, int cf_bytes)
+{
+    const int N = c->model.n_params, NF = c->n_filters;
+    FitBuffers& b = c->fb;
+    const int64_t S = (slots + 31) / 32 * 32;
+    if (b.base && b.slots_pad >= S && b.chains >= chains && b.groups >= groups && b.n_params == N &&
+        b.n_filters == NF && b.cf_bytes == cf_bytes) {
+        b.slots = slots;
+        return AST_OK;
+    }
+    ast_fit_free(c);
+    auto al = [](int64_t v) { return (v + 255) / 256 * 256; };
+    int64_t o = 0;
+    const int64_t o_x = o; o += al(S * (N + 1) * N * cf_bytes);
+    const int64_t o_f = o; o += al(S * (N + 1) * cf_bytes);
+    const int64_t o_ind = o; o += al(S * (N + 1));
+    const int64_t o_x0 = o; o += al(S * N * cf_bytes);
+    const int64_t o_xr = o; o += al(S * N * cf_bytes);
+    const int64_t o_fr = o; o += al(S * cf_bytes);
+    const int64_t o_st = o; o += al(S * 4);
+    const int64_t o_it = o; o += al(S * 4);
+    const int64_t o_ev = o; o += al(S * 4);
+    const int64_t o_ch = o; o += al(S * 8);
+    const int64_t o_dv = o; o += al(S * NF * 8);
+    const int64_t o_cf = o; o += al(chains * 8);
+    const int64_t o_cx = o; o += al(chains * N * cf_bytes);
+    const int64_t o_cdv = o; o += al(chains * NF * 8);
+    const int64_t o_gx = o; o += al(groups * N * cf_bytes);
+    const int64_t o_of = o; o += al(groups * 8);
+    const int64_t o_op = o; o += al(groups * N * 8);
+    const int64_t o_odv = o; o += al(groups * NF * 8);
+    const int64_t o_ctr = o; o += al(8 * 8);
+    void* base = nullptr;
+    if (cudaMalloc(&base, (size_t)o) != cudaSuccess) {
+        cudaGetLastError();
+        return ast_set_error(AST_E_NOMEM, "fit: cudaMalloc(%lld bytes) for %lld slots / %lld chains failed",
+                             (long long)o, (long long)slots, (long long)chains);
+    }
+    char* p = (char*)base;
+    b.base = base;
+    b.bytes = (size_t)o;
+    b.x = p + o_x; b.f = p + o_f; b.ind = (uint8_t*)(p + o_ind); b.x0 = p + o_x0; b.xr = p + o_xr; b.fr = p + o_fr;
+    b.st = (int32_t*)(p + o_st); b.it = (int32_t*)(p + o_it); b.ev = (int32_t*)(p + o_ev);
+    b.chain = (int64_t*)(p + o_ch); b.dv = (double*)(p + o_dv);
+    b.chain_f = (double*)(p + o_cf); b.chain_x = p + o_cx; b.chain_dv = (double*)(p + o_cdv);
+    b.group_x = p + o_gx; b.out_f = (double*)(p + o_of); b.out_p = (double*)(p + o_op); b.out_dv = (double*)(p + o_odv);
+    b.ctr = (unsigned long long*)(p + o_ctr);
+    b.slots = slots; b.slots_pad = S; b.chains = chains; b.groups = groups;
+    b.n_params = N; b.n_filters = NF; b.cf_bytes = cf_bytes;
+    return AST_OK;
+}
+
+template <class CF, int PREC>
+static int fit_launch_cfg(ast_ctx* c, int tpb_req, int64_t n_chains, int* tpb_out, int* ctas_out, size_t* smem_out)
+{
+    const size_t smem = ast_obs_smem(c);
+    auto kern = fit_kernel<CF, PREC>;
+    if (smem) AST_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int tpb = tpb_req;
+    if (tpb <= 0) {
+        // Enough CTAs to cover every SM before growing the CTA (small chain counts).
+        int64_t per_sm = n_chains / (c->sm_count > 0 ? c->sm_count : 1);
+        tpb = 32;
+        while (tpb < 256 && tpb * 2 <= per_sm) tpb *= 2;
+    }
+    if (tpb < 32 || tpb > 256 || (tpb & 31)) return ast_set_error(AST_E_INVALID, "fit: tpb must be 32..256, multiple of 32");
+    int occ = 1;
+    AST_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, tpb, smem));
+    if (occ < 1) return ast_set_error(AST_E_TOO_LARGE, "fit: kernel does not fit on an SM with %zu B shared memory", smem);
+    int64_t ctas = (int64_t)c->sm_count * occ;
+    const int64_t need = (n_chains + tpb - 1) / tpb;
+    if (ctas > need) ctas = need;
+    if (ctas < 1) ctas = 1;
+    *tpb_out = tpb;
+    *ctas_out = (int)ctas;
+    *smem_out = smem;
+    return AST_OK;
+}
+
+extern "C" int ast_fit_begin(ast_ctx* c, const ast_fit_cfg* cfg)
+{
+    if (!c || !cfg) return ast_set_error(AST_E_INVALID, "ast_fit_begin: NULL argument");
+    if (cfg->n_chains <= 0 || cfg->group_size <= 0 || cfg->n_chains % cfg->group_size)
+        return ast_set_error(AST_E_INVALID, "ast_fit_begin: n_chains must be a positive multiple of group_size");
+    if (cfg->n_stages <= 0) return ast_set_error(AST_E_INVALID, "ast_fit_begin: n_stages must be >= 1");
+    if (cfg->precision != AST_PREC_FP64 && cfg->precision != AST_PREC_MIXED)
+        return ast_set_error(AST_E_INVALID, "ast_fit_begin: bad precision");
+    if (cfg->reopt && !cfg->params0) return ast_set_error(AST_E_INVALID, "ast_fit_begin: reopt needs params0");
+    if (cfg->n_stages > 1 && cfg->n_stages > 1000000) return ast_set_error(AST_E_INVALID, "ast_fit_begin: n_stages too large");
+    int rc = set_device(c->device);
+    if (rc) return rc;
+    FitRun& r = c->run;
+    r = FitRun();
+    r.cfg = *cfg;
+    r.cfg.params0 = nullptr;
+    r.stage = 0;
+    r.reopt = cfg->reopt ? 1 : 0;
+    const bool acc = (c->model.flags & AST_ACC) != 0;
+    const int cfb = acc ? 8 : 4;
+    if (acc)
+        rc = cfg->precision == AST_PREC_FP64 ? fit_launch_cfg<double, AST_PREC_FP64>(c, cfg->tpb, cfg->n_chains, &r.tpb, &r.ctas, &r.smem)
+                                             : fit_launch_cfg<double, AST_PREC_MIXED>(c, cfg->tpb, cfg->n_chains, &r.tpb, &r.ctas, &r.smem);
+    else
+        rc = cfg->precision == AST_PREC_FP64 ? fit_launch_cfg<float, AST_PREC_FP64>(c, cfg->tpb, cfg->n_chains, &r.tpb, &r.ctas, &r.smem)
+                                             : fit_launch_cfg<float, AST_PREC_MIXED>(c, cfg->tpb, cfg->n_chains, &r.tpb, &r.ctas, &r.smem);
+    if (rc) return rc;
+    const int64_t slots = (int64_t)r.tpb * r.ctas;
+    const int64_t groups = cfg->n_chains / cfg->group_size;
+    if ((rc = fit_alloc(c, slots, cfg->n_chains, groups, cfb))) return rc;
+    FitBuffers& b = c->fb;
+    AST_CUDA(cudaMemsetAsync(b.ctr, 0, 8 * 8, c->stream));
+    reset_slots_kernel<<<(unsigned)((b.slots_pad + 255) / 256), 256, 0, c->stream>>>(b.chain, b.st, b.it, b.ev, b.dv,
+                                                                                      b.slots_pad, c->n_filters);
+    AST_CUDA(cudaGetLastError());
+    AST_CUDA(cudaMemsetAsync(b.chain_dv, 0, sizeof(double) * cfg->n_chains * c->n_filters, c->stream));
+    if (cfg->reopt) {
+        // Stage-0 start of every group: params2x of the -m model (cuda.c:1409-1416).
+        const int N = c->model.n_params;
+        std::vector<double> x(N);
+        if ((rc = ast_params2x(&c->model, cfg->params0, x.data()))) return rc;
+        std::vector<unsigned char> gx((size_t)groups * N * cfb);
+        for (int64_t g = 0; g < groups; g++)
+            for (int i = 0; i < N; i++) {
+                if (acc) ((double*)gx.data())[g * N + i] = x[i];
+                else ((float*)gx.data())[g * N + i] = (float)x[i];
+            }
+        AST_CUDA(cudaMemcpyAsync(b.group_x, gx.data(), gx.size(), cudaMemcpyHostToDevice, c->stream));
+        AST_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    r.active = true;
+    return AST_OK;
+}
+
+template <class CF, int PREC>
+static int fit_step_t(ast_ctx* c, int64_t budget, int32_t* done, cudaStream_t s)
+{
+    FitRun& r = c->run;
+    FitBuffers& b = c->fb;
+    FitView<CF> V = make_view<CF>(c);
+    AST_CUDA(cudaEventRecord(c->ev0, s));
+    fit_kernel<CF, PREC><<<r.ctas, r.tpb, r.smem, s>>>(c->dm, c->d_obs, c->layout, r.smem ? 1 : 0, V, budget);
+    AST_CUDA(cudaGetLastError());
+    AST_CUDA(cudaEventRecord(c->ev1, s));
+    unsigned long long h[8];
+    AST_CUDA(cudaMemcpyAsync(h, b.ctr, sizeof(h), cudaMemcpyDeviceToHost, s));
+    AST_CUDA(cudaStreamSynchronize(s));
+    float ms = 0;
+    AST_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    r.kernel_ms += ms;
+    if (h[4]) return ast_set_error(AST_E_TIMEOUT, "fit: a CTA's shared-memory staging wait ran out (error word %llu)", h[4]);
+    if (h[1] < (unsigned long long)r.cfg.n_chains) {
+        *done = 0;
+        return AST_OK;
+    }
+    // Stage finished: group argmin, hand-off or output.
+    group_best_kernel<CF><<<(unsigned)b.groups, 256, 0, s>>>(c->dm, V, b.out_f, b.out_p, b.out_dv);
+    AST_CUDA(cudaGetLastError());
+    if (r.stage == r.cfg.n_stages - 1) {
+        *done = 1;
+        r.n_evals = (int64_t)h[2];
+        r.n_fits = (int64_t)h[3];
+        AST_CUDA(cudaStreamSynchronize(s));
+        return AST_OK;
+    }
+    r.stage++;
+    r.reopt = 1;
+    unsigned long long z[2] = {0, 0};
+    AST_CUDA(cudaMemcpyAsync(b.ctr, z, sizeof(z), cudaMemcpyHostToDevice, s));
+    AST_CUDA(cudaStreamSynchronize(s));
+    *done = 0;
+    return AST_OK;
+}
+
+extern "C" int ast_fit_step(ast_ctx* c, int64_t evals_per_slot, int32_t* done, void* stream)
+{
+    if (!c || !done) return ast_set_error(AST_E_INVALID, "ast_fit_step: NULL argument");
+    if (!c->run.active) return ast_set_error(AST_E_INVALID, "ast_fit_step: no fit begun");
+    if (evals_per_slot <= 0) evals_per_slot = INT64_MAX;
+    int rc = set_device(c->device);
+    if (rc) return rc;
+    cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
+    const bool acc = (c->model.flags & AST_ACC) != 0;
+    if (c->run.cfg.precision == AST_PREC_FP64)
+        return acc ? fit_step_t<double, AST_PREC_FP64>(c, evals_per_slot, done, s)
+                   : fit_step_t<float, AST_PREC_FP64>(c, evals_per_slot, done, s);
+    return acc ? fit_step_t<double, AST_PREC_MIXED>(c, evals_per_slot, done, s)
+               : fit_step_t<float, AST_PREC_MIXED>(c, evals_per_slot, done, s);
+}
+
+extern "C" int ast_fit_counters(ast_ctx* c, int64_t* n_evals, int64_t* n_fits)
+{
+    if (!c || !c->fb.ctr) return ast_set_error(AST_E_INVALID, "ast_fit_counters: no fit");
+    unsigned long long h[8];
+    AST_CUDA(cudaMemcpyAsync(h, c->fb.ctr, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    AST_CUDA(cudaStreamSynchronize(c->stream));
+    if (n_evals) *n_evals = (int64_t)h[2];
+    if (n_fits) *n_fits = (int64_t)h[3];
+    return AST_OK;
+}
+
+extern "C" int64_t ast_fit_slots(ast_ctx* c) { return c ? c->fb.slots : 0; }
+
+extern "C" int ast_fit_end(ast_ctx* c, ast_fit_out* out)
+{
+    if (!c || !out) return ast_set_error(AST_E_INVALID, "ast_fit_end: NULL argument");
+    if (!c->run.active) return ast_set_error(AST_E_INVALID, "ast_fit_end: no fit begun");
+    int rc = set_device(c->device);
+    if (rc) return rc;
+    FitBuffers& b = c->fb;
+    const int N = c->model.n_params, NF = c->n_filters;
+    const int64_t G = c->run.cfg.n_chains / c->run.cfg.group_size;
+    unsigned long long h[8];
+    AST_CUDA(cudaMemcpyAsync(h, b.ctr, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    if (out->best_f) AST_CUDA(cudaMemcpyAsync(out->best_f, b.out_f, sizeof(double) * G, cudaMemcpyDeviceToHost, c->stream));
+    if (out->best_params)
+        AST_CUDA(cudaMemcpyAsync(out->best_params, b.out_p, sizeof(double) * G * N, cudaMemcpyDeviceToHost, c->stream));
+    if (out->best_dv)
+        AST_CUDA(cudaMemcpyAsync(out->best_dv, b.out_dv, sizeof(double) * G * NF, cudaMemcpyDeviceToHost, c->stream));
+    if (out->chain_f)
+        AST_CUDA(cudaMemcpyAsync(out->chain_f, b.chain_f, sizeof(double) * c->run.cfg.n_chains, cudaMemcpyDeviceToHost,
+                                 c->stream));
+    AST_CUDA(cudaStreamSynchronize(c->stream));
+    out->n_evals = c->run.n_evals ? c->run.n_evals : (int64_t)h[2];
+    out->n_fits = c->run.n_fits ? c->run.n_fits : (int64_t)h[3];
+    out->kernel_ms = c->run.kernel_ms;
+    c->run.active = false;
+    return AST_OK;
+}
+
+extern "C" int ast_fit(ast_ctx* c, const ast_fit_cfg* cfg, ast_fit_out* out)
+{
+    int rc = ast_fit_begin(c, cfg);
+    if (rc) return rc;
+    int32_t done = 0;
+    for (int guard = 0; !done; guard++) {
+        if ((rc = ast_fit_step(c, 0, &done, nullptr))) return rc;
+        if (guard > 4 * cfg->n_stages + 16)
+            return ast_set_error(AST_E_TIMEOUT, "ast_fit: stages did not complete");
+    }
+    return ast_fit_end(c, out);
+}

@@ -1,0 +1,291 @@
+// mixed.cuh -- the mixed-precision chi^2: FP32 right-hand side and brightness, FP64 state.
+//
+// GB300 runs FP32 FMAs at 64x the FP64 rate, so the plain path is bound by the FP64 pipe.
+// Here the Euler-equation / Euler-angle right-hand side (cuda.c:44-75) and the brightness
+// model (cuda.c:432-689) are evaluated in FP32 from angles first reduced to [-pi, pi) in
+// FP64, while the RK4 state and its stage updates stay in FP64 (rotation phase grows to
+// ~1e5 rad over a long light curve, where one FP32 ulp is ~0.008 rad), and the per-filter
+// sums and the chi^2 are accumulated in FP64.  Error against the FP64 path is measured by
+// tests/test_mixed.py and reported by bench.py.
+#pragma once
+#include <math.h>
+#include "model.cuh"
+
+namespace ast {
+
+// x reduced to [-pi, pi) in FP64 with a two-term 2*pi (Cody-Waite), then rounded to FP32.
+__device__ __forceinline__ float reduce_angle_f(double x)
+{
+    const double k = rint(x * 0.15915494309189535);       // 1 / (2 pi)
+    const double r = fma(-k, 6.283185307179586, x);        // 2 pi, high part
+    return (float)fma(-k, 2.4492935982947064e-16, r);      // 2 pi, low part
+}
+
+__device__ __forceinline__ void ode_torque_f(const double* y, float* f, const float* mu)
+{
+    float s5, c5, s4, c4;
+    sincosf(reduce_angle_f(y[5]), &s5, &c5);
+    sincosf(reduce_angle_f(y[4]), &s4, &c4);
+    const float y0 = (float)y[0], y1 = (float)y[1], y2 = (float)y[2];
+    f[0] = mu[0] * y1 * y2 + mu[3];
+    f[1] = mu[1] * y2 * y0 + mu[4];
+    f[2] = mu[2] * y0 * y1 + mu[5];
+    f[3] = (y0 * s5 + y1 * c5) / s4;
+    f[4] = y0 * c5 - y1 * s5;
+    f[5] = y2 - f[3] * c4;
+}
+
+__device__ __forceinline__ void ode_free_f(const double* y, float* f, const float* mu)
+{
+    float s2, c2, s1, c1;
+    sincosf(reduce_angle_f(2.0 * y[2]), &s2, &c2);
+    sincosf(reduce_angle_f(y[1]), &s1, &c1);
+    f[0] = mu[0] * (mu[1] - mu[2] * c2);
+    f[1] = mu[0] * mu[2] * s1 * s2;
+    f[2] = c1 * (mu[0] - f[0]);
+}
+
+template <int NODE>
+__device__ __forceinline__ void rk4_step_mixed(double* y, double h, const float* mu)
+{
+    double f[NODE];
+    float K1[NODE], K2[NODE], K3[NODE], K4[NODE];
+    const double hh = 0.5 * h;
+    if (NODE == 6) ode_torque_f(y, K1, mu); else ode_free_f(y, K1, mu);
+#pragma unroll
+    for (int j = 0; j < NODE; j++) f[j] = fma(hh, (double)K1[j], y[j]);
+    if (NODE == 6) ode_torque_f(f, K2, mu); else ode_free_f(f, K2, mu);
+#pragma unroll
+    for (int j = 0; j < NODE; j++) f[j] = fma(hh, (double)K2[j], y[j]);
+    if (NODE == 6) ode_torque_f(f, K3, mu); else ode_free_f(f, K3, mu);
+#pragma unroll
+    for (int j = 0; j < NODE; j++) f[j] = fma(h, (double)K3[j], y[j]);
+    if (NODE == 6) ode_torque_f(f, K4, mu); else ode_free_f(f, K4, mu);
+    const double h6 = h * (1 / 6.0);
+#pragma unroll
+    for (int j = 0; j < NODE; j++) y[j] = fma(h6, (double)(K1[j] + 2.0f * (K2[j] + K3[j]) + K4[j]), y[j]);
+}
+
+// Same contract as chi2_fp64 (model.cuh).
+template <class CF>
+__device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const double* params, CF* delta_V)
+{
+    const int flags = M.flags;
+    const ast_type_ids& T = M.t;
+    const int N_data = M.n_data, N_filters = M.n_filters;
+    double sum_y2[AST_MAX_FILTERS], sum_y[AST_MAX_FILTERS], sum_w[AST_MAX_FILTERS];
+    for (int m = 0; m < N_filters; m++) { sum_y2[m] = 0.0; sum_y[m] = 0.0; sum_w[m] = 0.0; }
+    int Mmin = 0;
+    float t_mod[AST_M_MAX], V_mod[AST_M_MAX];
+    float t_old[2] = {0.f, 0.f}, V_old[2] = {0.f, 0.f};
+
+#define AST_P(tt) params[M.idx[T.tt]]
+    // Parameter-level set-up in FP64 (once per evaluation).
+    const double th_M = AST_P(theta_M), ph_M = AST_P(phi_M);
+    const double M_xd = sin(th_M) * cos(ph_M), M_yd = sin(th_M) * sin(ph_M), M_zd = cos(th_M);
+    const double XMd = sqrt(M_zd * M_zd + M_xd * M_xd);
+    const float M_x = (float)M_xd, M_y = (float)M_yd, M_z = (float)M_zd;
+    const float XM_x = (float)(M_zd / XMd), XM_z = (float)(-M_xd / XMd);
+    const float YM_x = M_y * XM_z, YM_y = M_z * XM_x - M_x * XM_z, YM_z = -M_y * XM_x;
+    const double bt = AST_P(b_tumb), ct = AST_P(c_tumb);
+    const double Is = (1.0 + bt * bt) / (bt * bt + ct * ct);
+    const double Ii = (1.0 + ct * ct) / (bt * bt + ct * ct);
+    const double Is_inv = 1.0 / Is, Ii_inv = 1.0 / Ii;
+    const double psi0 = AST_P(psi_0);
+    double y[6];
+    float mu[6];
+    const bool torque = (flags & AST_TORQUE) != 0;
+    {
+        const double theta = asin(sqrt((AST_P(Es) - 1.0) / (sin(psi0) * sin(psi0) * (Ii_inv - Is_inv) + Is_inv - 1.0)));
+        if (torque) {
+            mu[0] = (float)((Is - 1.0) * Ii_inv);
+            mu[1] = (float)((1.0 - Ii) * Is_inv);
+            mu[2] = (float)(Ii - Is);
+            mu[3] = (float)AST_P(Ti);
+            mu[4] = (float)AST_P(Ts);
+            mu[5] = (float)AST_P(Tl);
+            const double L = AST_P(L);
+            y[0] = L * Ii_inv * sin(theta) * sin(psi0);
+            y[1] = L * Is_inv * sin(theta) * cos(psi0);
+            y[2] = L * cos(theta);
+            y[3] = AST_P(phi_0);
+            y[4] = theta;
+            y[5] = psi0;
+        } else {
+            mu[0] = (float)AST_P(L);
+            mu[1] = (float)(0.5 * (Ii_inv + Is_inv));
+            mu[2] = (float)(0.5 * (Ii_inv - Is_inv));
+            y[0] = AST_P(phi_0);
+            y[1] = theta;
+            y[2] = psi0;
+        }
+    }
+    const bool bw = (flags & AST_BW_BALL) != 0;
+    float b_ph = 0, c_ph = 0, kappa = 0, cos_phR = 0, sin_phR = 0, cos_thR = 0, sin_thR = 0;
+    if (bw) {
+        kappa = (float)AST_P(kappa);
+        sincosf((float)AST_P(phi_R), &sin_phR, &cos_phR);
+        sincosf((float)AST_P(theta_R), &sin_thR, &cos_thR);
+    } else {
+        b_ph = (float)((flags & AST_BC) ? AST_P(b) : bt);
+        c_ph = (float)((flags & AST_BC) ? AST_P(c) : ct);
+    }
+    const float ib2 = 1.0f / (b_ph * b_ph), ic2 = 1.0f / (c_ph * c_ph);
+
+    for (int i = 0; i < N_data; i++) {
+        if (i > 0) {
+            const int N_steps = o.nst[i];
+            const double h = o.h[i];
+            if (torque)
+                for (int l = 0; l < N_steps; l++) rk4_step_mixed<6>(y, h, mu);
+            else
+                for (int l = 0; l < N_steps; l++) rk4_step_mixed<3>(y, h, mu);
+        }
+        float sin_phi, cos_phi, sin_theta, cos_theta, sin_psi, cos_psi;
+        sincosf(reduce_angle_f(torque ? y[3] : y[0]), &sin_phi, &cos_phi);
+        sincosf(reduce_angle_f(torque ? y[4] : y[1]), &sin_theta, &cos_theta);
+        sincosf(reduce_angle_f(torque ? y[5] : y[2]), &sin_psi, &cos_psi);
+        float N_x = XM_x * cos_phi + YM_x * sin_phi;
+        float N_y = YM_y * sin_phi;
+        float N_z = XM_z * cos_phi + YM_z * sin_phi;
+        float p_x = N_y * M_z - N_z * M_y;
+        float p_y = N_z * M_x - N_x * M_z;
+        float p_z = N_x * M_y - N_y * M_x;
+        float a_x = M_x * cos_theta + p_x * sin_theta;
+        float a_y = M_y * cos_theta + p_y * sin_theta;
+        float a_z = M_z * cos_theta + p_z * sin_theta;
+        const float w_x = a_y * N_z - a_z * N_y;
+        const float w_y = a_z * N_x - a_x * N_z;
+        const float w_z = a_x * N_y - a_y * N_x;
+        const float b_x = N_x * cos_psi + w_x * sin_psi;
+        const float b_y = N_y * cos_psi + w_y * sin_psi;
+        const float b_z = N_z * cos_psi + w_z * sin_psi;
+        const float c_x = a_y * b_z - a_z * b_y;
+        const float c_y = a_z * b_x - a_x * b_z;
+        const float c_z = a_x * b_y - a_y * b_x;
+        const float E_x1 = (float)o.ex[i], E_y1 = (float)o.ey[i], E_z1 = (float)o.ez[i];
+        const float S_x1 = (float)o.sx[i], S_y1 = (float)o.sy[i], S_z1 = (float)o.sz[i];
+        float Vmod;
+        if (bw) {
+            N_x = b_x * cos_phR + c_x * sin_phR;
+            N_y = b_y * cos_phR + c_y * sin_phR;
+            N_z = b_z * cos_phR + c_z * sin_phR;
+            p_x = N_y * a_z - N_z * a_y;
+            p_y = N_z * a_x - N_x * a_z;
+            p_z = N_x * a_y - N_y * a_x;
+            a_x = a_x * cos_thR + p_x * sin_thR;
+            a_y = a_y * cos_thR + p_y * sin_thR;
+            a_z = a_z * cos_thR + p_z * sin_thR;
+            const float cos_zeta = a_x * E_x1 + a_y * E_y1 + a_z * E_z1;
+            Vmod = -2.5f * log10f(0.5f * (kappa * (1 + cos_zeta) + 0.5f * (1 - cos_zeta)));
+        } else {
+            const float Ep_b = b_x * E_x1 + b_y * E_y1 + b_z * E_z1;
+            const float Ep_c = c_x * E_x1 + c_y * E_y1 + c_z * E_z1;
+            const float Ep_a = a_x * E_x1 + a_y * E_y1 + a_z * E_z1;
+            const float Sp_b = b_x * S_x1 + b_y * S_y1 + b_z * S_z1;
+            const float Sp_c = c_x * S_x1 + c_y * S_y1 + c_z * S_z1;
+            const float Sp_a = a_x * S_x1 + a_y * S_y1 + a_z * S_z1;
+            const float sS = sqrtf(Sp_b * Sp_b * ib2 + Sp_c * Sp_c * ic2 + Sp_a * Sp_a);
+            const float sE = sqrtf(Ep_b * Ep_b * ib2 + Ep_c * Ep_c * ic2 + Ep_a * Ep_a);
+            const float cos_alpha_p = (Sp_b * Ep_b * ib2 + Sp_c * Ep_c * ic2 + Sp_a * Ep_a) / (sS * sE);
+            const float sin_alpha_p = sqrtf(fmaxf(0.0f, 1.0f - cos_alpha_p * cos_alpha_p));
+            const float alpha_p = atan2f(sin_alpha_p, cos_alpha_p);
+            const float scalar = sqrtf(sS * sS + sE * sE + 2 * sS * sE * cos_alpha_p);
+            const float cos_lambda_p = (sS + sE * cos_alpha_p) / scalar;
+            const float sin_lambda_p = sE * sin_alpha_p / scalar;
+            const float lambda_p = atan2f(sin_lambda_p, cos_lambda_p);
+            float s_la, c_la;
+            sincosf(lambda_p - alpha_p, &s_la, &c_la);
+            Vmod = -2.5f * log10f(b_ph * c_ph * sS * sE / scalar *
+                                  (c_la + cos_lambda_p +
+                                   sin_lambda_p * s_la * logf(1.0f / tanf(0.5f * lambda_p) / tanf(0.5f * (alpha_p - lambda_p)))));
+        }
+        {
+            const int m = o.f[i];
+            const double yv = (double)o.v[i] - (double)Vmod;
+            const double wi = o.w[i];
+            sum_y2[m] = fma(yv * yv, wi, sum_y2[m]);
+            sum_y[m] = fma(yv, wi, sum_y[m]);
+            sum_w[m] = sum_w[m] + wi;
+        }
+        if (flags & AST_NUDGE) {
+            if (i < 2) {
+                t_old[i] = (float)o.t[i];
+                V_old[i] = Vmod;
+            } else {
+                if (V_old[1] > V_old[0] && V_old[1] >= Vmod) {
+                    bool local = false;
+                    for (int ii = 0; ii < M.n_min; ii++)
+                        if (fabsf(t_old[1] - M.t_min[ii]) < AST_DT_MAX2) local = true;
+                    if (local) {
+                        Mmin++;
+                        if (Mmin > AST_M_MAX) return (CF)kHuge;
+                        const double ti = o.t[i];
+                        const double a = (((double)Vmod - V_old[1]) / (ti - t_old[1]) - (V_old[1] - V_old[0]) / (t_old[1] - t_old[0])) / (ti - t_old[0]);
+                        const double b = (V_old[1] - V_old[0]) / (t_old[1] - t_old[0]) - a * (t_old[1] + t_old[0]);
+                        const double c = V_old[1] - a * t_old[1] * t_old[1] - b * t_old[1];
+                        t_mod[Mmin - 1] = (float)(-b / 2.0 / a);
+                        V_mod[Mmin - 1] = (float)(a * t_mod[Mmin - 1] * t_mod[Mmin - 1] + b * t_mod[Mmin - 1] + c);
+                    }
+                }
+                t_old[0] = t_old[1];
+                V_old[0] = V_old[1];
+                t_old[1] = (float)o.t[i];
+                V_old[1] = Vmod;
+            }
+        }
+    }
+#undef AST_P
+    CF chi2m, chi2a = 0.0;
+    CF dv[AST_MAX_FILTERS];
+    for (int m = 0; m < N_filters; m++) {
+        chi2m = (CF)(sum_y2[m] - sum_y[m] * sum_y[m] / sum_w[m]);
+        chi2a = chi2a + chi2m;
+        dv[m] = (CF)(sum_y[m] / sum_w[m]);
+    }
+    chi2a = chi2a / (CF)(N_data - M.n_params - N_filters);
+    if (flags & AST_NUDGE) {
+        float S_M = 0.0f, P_tot = 1.0f;
+        for (int imod = 0; imod < Mmin; imod++) {
+            for (int iobs = 0; iobs < M.n_min; iobs++) {
+                const float dt = fabsf(t_mod[imod] - M.t_min[iobs]);
+                if (dt < AST_DT_MAX2) {
+                    if (dt > AST_DT_MAX) {
+                        const float x = (AST_DT_MAX2 - dt) / (AST_DT_MAX2 - AST_DT_MAX);
+                        S_M = (float)(S_M + x * x * (-2.0 * x + 3.0));
+                    } else {
+                        S_M = (float)(S_M + 1.0);
+                        const float dV = (float)(V_mod[imod] + dv[0] - M.v_min[iobs]);
+                        const float x = sqrtf(dt * dt / AST_DT_MAX / AST_DT_MAX + dV * dV / AST_DV_MAX / AST_DV_MAX);
+                        if (x < 1.0f) {
+                            const float P_i = AST_L_A * x * x / (x * x + AST_L_RC2);
+                            P_tot = (float)(P_tot * (AST_P_MIN * (1.0 + AST_P_MIN2 * P_i)));
+                        }
+                    }
+                }
+            }
+        }
+        P_tot = powf(P_tot, (float)(1.0 / M.n_min));
+        if (P_tot < AST_P_MIN) P_tot = AST_P_MIN;
+        if (chi2a > AST_CHI2_1)
+            P_tot = 1.0f;
+        else if (chi2a > AST_CHI2_0) {
+            const float x = (float)((AST_CHI2_1 - chi2a) / (AST_CHI2_1 - AST_CHI2_0));
+            const float beta = x * x * (-2 * x + 3);
+            P_tot = powf(P_tot, beta);
+        }
+        float P_M;
+        if (S_M < AST_M_MAX2)
+            P_M = 1.0f;
+        else if (S_M < AST_M_MAX) {
+            const float x = (S_M - AST_M_MAX2) / (AST_M_MAX - AST_M_MAX2);
+            P_M = (float)(1.0 + 3 * x * x * (-2 * x + 3));
+        } else
+            P_M = 4.0f;
+        chi2a = chi2a * P_tot * P_M;
+    }
+    for (int m = 0; m < N_filters; m++) delta_V[m] = dv[m];
+    return chi2a;
+}
+
+}  // namespace ast

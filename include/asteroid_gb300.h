@@ -1,0 +1,269 @@
+/*
+ * asteroid_gb300.h -- C ABI of the GB300 (sm_103a) light-curve fitting engine.
+ *
+ * The engine evaluates the chi^2 of a tumbling, optionally torqued asteroid model against a
+ * photometric light curve, and runs downhill-simplex (Nelder-Mead) chains with random starts
+ * on the device.  It is a drop-in for the fitting path of pulsar123/Asteroid:
+ *
+ *   reference interface (file:line in the Asteroid sources)      replaced here by
+ *   --------------------------------------------------------      ----------------------------
+ *   gpu_prepare(N_data,N_filters,N_threads,Nplot)  gpu_prepare.c:2  ast_prepare()
+ *   cudaMemcpyToSymbol(dProperty,dTypes,dLimits,d_x2_params)
+ *                                              asteroid.c:603-606  ast_set_tables()
+ *   prepare_chi2_params() (observed.min upload)   misc.c:279-323  ast_obs_set.n_minima/t_min/v_min
+ *   chi2one(params,sData,...)  (one chi^2 evaluation) cuda.c:81    ast_eval_batch()
+ *   setup_kernel + chi2_gpu<<<N_BLOCKS,BSIZE>>>  cuda.c:2039,1326   ast_fit() / ast_fit_begin/step/end
+ *   cudaMemcpy D2H of d_params,d_dV,d_f           asteroid.c:728-730 ast_fit_out (caller buffers)
+ *   ERR() -> gpuAssert -> exit                     cuda_errors.h:4-14 int status + ast_last_error()
+ *   read_data()                                    read_data.c:6     ast_read_data()
+ *   quadratic_interpolation()                      misc.c:20         ast_quadratic_interpolation()
+ *   Property/Types/hLimits tables                  asteroid.c:86-169,473-601  ast_model_init()
+ *
+ * All entry points take plain pointers and sizes.  Every function returns 0 on success or a
+ * negative AST_E_* status; ast_last_error() gives a message for the calling thread.
+ * A context is single-threaded: calls on one ast_ctx must not overlap.  All calls block until
+ * their results are in the caller's buffers, except the *_device variants, which are
+ * stream-ordered on the stream passed in.
+ */
+#ifndef ASTEROID_GB300_H
+#define ASTEROID_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- sizes */
+#define AST_MAX_PARAMS   16   /* N_PARAMS of every supported variant is <= 14 */
+#define AST_MAX_TYPES    16
+#define AST_MAX_FILTERS  8    /* N_FILTERS (asteroid.h:191) is a runtime value here */
+#define AST_NOBS_MAX     10   /* observed minima, asteroid.h:219 */
+#define AST_M_MAX        30   /* model minima, asteroid.h:217 */
+#define AST_N_COLUMNS    6
+#define AST_MAX_DATA     16384 /* observations per object (staged tile-wise when large) */
+
+/* ---------------------------------------------------------------- status codes */
+#define AST_OK             0
+#define AST_E_INVALID     -1   /* bad argument / inconsistent input */
+#define AST_E_NOMEM       -2   /* device or host allocation failed */
+#define AST_E_CUDA        -3   /* CUDA runtime error (message in ast_last_error) */
+#define AST_E_IO          -4   /* file missing or malformed */
+#define AST_E_TOO_LARGE   -5   /* size beyond a documented maximum */
+#define AST_E_BUDGET      -6   /* request does not fit the admission budget */
+#define AST_E_TIMEOUT     -7   /* a device wait gave up after its iteration limit */
+#define AST_E_NOT_READY   -8   /* result not available yet */
+#define AST_E_NODEVICE    -9   /* no CUDA device */
+
+/* ---------------------------------------------------------------- model variants
+ * The reference selects these with compile-time macros (makefile:1-36); here they are
+ * runtime flags of an ast_model.  Parameter order and type numbering follow the reference
+ * for every combination (asteroid.c:86-125, asteroid.h:137-178). */
+#define AST_TORQUE   0x01  /* -DTORQUE : constant body-frame torque, 3 extra parameters */
+#define AST_BC       0x02  /* -DBC     : photometric c, b independent of c_tumb, b_tumb */
+#define AST_BW_BALL  0x04  /* -DBW_BALL: black-and-white ball brightness, theta_R phi_R kappa */
+#define AST_P_PSI    0x08  /* -DP_PSI  : L is generated from the Ppsi period range */
+#define AST_INTERP   0x10  /* -DINTERP : E,S from the 3-point ephemeris at asteroid time */
+#define AST_ACC      0x20  /* -DACC    : CHI_FLOAT = double, SIZE_MIN = 1e-10 */
+#define AST_NUDGE    0x40  /* -DNUDGE  : reward for model minima near observed minima */
+
+/* Property table columns (asteroid.h:115-123) */
+#define AST_P_TYPE          0
+#define AST_P_INDEPENDENT   1
+#define AST_P_FROZEN        2
+#define AST_P_ISEG          3
+#define AST_P_MULTI_SEGMENT 4
+#define AST_P_PERIODIC      5
+/* P_periodic values (asteroid.h:126-131) */
+#define AST_PERIODIC       1
+#define AST_PERIODIC_LAM   0
+#define AST_SOFT_BOTH     -1
+#define AST_HARD_LEFT     -2
+#define AST_HARD_RIGHT    -3
+#define AST_HARD_BOTH     -4
+
+/* Parameter type ids of one variant: the reference numbers types with __COUNTER__ in the
+ * order theta_M, phi_M, phi_0, L, [Ti Ts Tl], c_tumb, b_tumb, Es, psi_0, [c b],
+ * [theta_R phi_R], [kappa] (asteroid.h:137-178).  Absent types are -1.  These ids are
+ * what the -f and -l command-line switches take. */
+typedef struct ast_type_ids {
+    int32_t theta_M, phi_M, phi_0, L, Ti, Ts, Tl, c_tumb, b_tumb, Es, psi_0, c, b,
+            theta_R, phi_R, kappa;
+    int32_t n_types;
+} ast_type_ids;
+
+/* One model variant with its tables; the device copy of the reference's dProperty,
+ * dTypes, dLimits and d_x2_params symbols (asteroid.h:460,509-510,533). */
+typedef struct ast_model {
+    int32_t flags;                                   /* AST_TORQUE | ... */
+    int32_t n_params;                                /* N_PARAMS (asteroid.h:110) */
+    int32_t n_types;                                 /* N_TYPES  (asteroid.h:178) */
+    int32_t property[AST_MAX_PARAMS][AST_N_COLUMNS]; /* Property (asteroid.c:86-125) */
+    int32_t types[AST_MAX_TYPES];                    /* Types[type][0]: parameter index or -1 */
+    double  limits[2][AST_MAX_TYPES];                /* hLimits; float-rounded unless AST_ACC */
+    float   ppsi1, ppsi2;                            /* x2_struct.Ppsi1/2 = 24/Ppsi_max, 24/Ppsi_min */
+    double  time_step;                               /* TIME_STEP, days (asteroid.h:202) */
+    ast_type_ids ids;
+} ast_model;
+
+/* One object's light curve after the reference's host conversion (read_data.c:243-302):
+ * times are asteroid times minus the first one (hMJD0), magnitudes are geometry corrected,
+ * E and S are unit asteroid->Earth and asteroid->Sun vectors. */
+typedef struct ast_obs_set {
+    int32_t n_data;                 /* observations, >= n_params + n_filters + 1 */
+    int32_t n_filters;              /* distinct filters, <= AST_MAX_FILTERS */
+    const double*  mjd;             /* [n_data] days, strictly increasing */
+    const float*   v;               /* [n_data] magnitude (obs_data.V is float) */
+    const float*   w;               /* [n_data] 1/sgm^2    (obs_data.w is float) */
+    const int32_t* filter;          /* [n_data] 0..n_filters-1 */
+    const double*  e_unit;          /* [n_data*3] (x,y,z) per point; unused under AST_INTERP */
+    const double*  s_unit;          /* [n_data*3] */
+    double eph_e[3][3];             /* AST_INTERP: E_x0[3],E_y0[3],E_z0[3] (read_data.c:189-191) */
+    double eph_s[3][3];             /*             S_x0[3],S_y0[3],S_z0[3] */
+    double eph_mjd0[3];             /*             MJD0[3] minus hMJD0 (read_data.c:298-302) */
+    int32_t n_minima;               /* AST_NUDGE: observed minima (misc.c:279-323) */
+    float   t_min[AST_NOBS_MAX];    /*   minimum time minus hMJD0 */
+    float   v_min[AST_NOBS_MAX];    /*   minimum magnitude */
+} ast_obs_set;
+
+/* ---------------------------------------------------------------- tables (host, C) */
+
+/* Fill the Property/Types/hLimits tables of a variant exactly as asteroid.c:86-169 and
+ * :473-564 do, and the P_PSI range as asteroid.c:598-601 (ppsi_* in hours; ignored unless
+ * AST_P_PSI).  Replaces the table set-up at the top of the reference's main(). */
+int ast_model_init(ast_model* m, int32_t flags, double time_step,
+                   double ppsi_min_hours, double ppsi_max_hours);
+/* -f type value: freeze every parameter of that type at value (asteroid.c:566-581). */
+int ast_model_freeze(ast_model* m, int32_t type, double value);
+/* -l type l0 l1: custom limits for a type (asteroid.c:583-589). */
+int ast_model_set_limits(ast_model* m, int32_t type, double l0, double l1);
+/* -m ... "v": parameter randomly varied over its full range under -reopt (asteroid.c:310-315). */
+int ast_model_set_free_random(ast_model* m, int32_t param_index);
+/* Name of parameter i in output order (README.md:110-115 order), e.g. "theta_M". */
+const char* ast_param_name(const ast_model* m, int32_t i);
+
+/* x2params (cuda.c:1120-1319) on the host, with the model's CHI_FLOAT rounding of x:
+ * returns 0, 1 when x leaves a hard limit (the reference's failure), or a negative status.
+ * reopt selects the meaning of the L coordinate under P_PSI (cuda.c:1219,1244). */
+int ast_x2params(const ast_model* m, int32_t reopt, const double* x, double* params);
+/* params2x (cuda.c:1016-1115) on the host. */
+int ast_params2x(const ast_model* m, const double* params, double* x);
+
+/* ---------------------------------------------------------------- host I/O (C) */
+
+/* Host copy of a light curve read from the reference's files. */
+typedef struct ast_host_data {
+    ast_obs_set obs;          /* pointers into the arrays below */
+    double* mjd; float* v; float* w; int32_t* filter; double* e_unit; double* s_unit;
+    double* mjd_obs;          /* observer times as read (MJD_obs) */
+    double  hmjd0;            /* first asteroid time (read_data.c:274-276) */
+    char    filters[AST_MAX_FILTERS]; /* filter characters in order of appearance */
+} ast_host_data;
+
+/* read_data.c:6-302: read "filter MJD V sgm aux" lines from lc_path and the HORIZONS
+ * vector files asteroid.eph, earth.eph, sun.eph from eph_dir; apply the geometry and
+ * light-time corrections, normalise E and S.  interp selects the INTERP time shift of
+ * the ephemeris points.  Rejects unsorted times and more than max_filters filters. */
+int ast_read_data(const char* lc_path, const char* eph_dir, int32_t interp,
+                  int32_t max_filters, ast_host_data** out);
+/* misc.c:279-323: read observed.min lines "MJD_min V_min" from path, keep those within
+ * 0.05 d of the data range, at most AST_NOBS_MAX, into d->obs.n_minima/t_min/v_min. */
+int ast_read_minima(const char* path, ast_host_data* d);
+void ast_free_host_data(ast_host_data* d);
+
+/* misc.c:20-35: second-order Lagrange interpolation of E and S at time t. */
+void ast_quadratic_interpolation(const double mjd0[3], const double e[3][3], const double s[3][3],
+                                 double t, double out_e[3], double out_s[3]);
+
+/* asteroid.c:798-811: one result line "chi2 dV_1..dV_Nf p_1..p_N\n" with the reference's
+ * "%13.6e " / "%15.11f " formats.  Returns the number of characters written. */
+int ast_format_result(char* buf, int64_t cap, double chi2, const double* dv, int32_t n_filters,
+                      const double* params, int32_t n_params);
+
+/* ---------------------------------------------------------------- device engine */
+
+typedef struct ast_ctx ast_ctx;
+
+#define AST_PREC_FP64   0   /* plain path: the reference's double arithmetic */
+#define AST_PREC_MIXED  1   /* FP32 right-hand side and brightness, double-FP32 state */
+
+/* gpu_prepare.c:2-56 + asteroid.c:603-606: pack one object's observations into SoA device
+ * buffers (16-byte aligned segments staged into shared memory by bulk copies), hoist the
+ * parameter-independent ephemeris interpolation, upload the tables.  device < 0 means the
+ * current device. */
+int ast_prepare(const ast_model* model, const ast_obs_set* obs, int32_t device, ast_ctx** out);
+/* Replace the tables after ast_prepare (same variant flags and n_params). */
+int ast_set_tables(ast_ctx* ctx, const ast_model* model);
+void ast_destroy(ast_ctx* ctx);
+const char* ast_last_error(void);
+
+/* chi2one (cuda.c:81-1011) on n physical parameter vectors params[n][n_params], host
+ * buffers.  chi2[n] receives the value chi2one returns (1e30 for the NUDGE failure),
+ * delta_v[n][n_filters] (may be NULL) the per-filter offsets.  Results follow CHI_FLOAT:
+ * rounded to float unless the model has AST_ACC. */
+int ast_eval_batch(ast_ctx* ctx, int32_t precision, const double* params, int64_t n,
+                   double* chi2, double* delta_v);
+/* Same with device pointers, stream-ordered on `stream` (a cudaStream_t; NULL = legacy). */
+int ast_eval_batch_device(ast_ctx* ctx, int32_t precision, const double* d_params, int64_t n,
+                          double* d_chi2, double* d_delta_v, void* stream);
+
+/* Model magnitude at every observation of the context's object for one parameter vector
+ * (the reference's chi2one with Nplot > 0, cuda.c:699-704, without the delta_V shift):
+ * the model-curve path of the plot mode and of the synthetic-data generator. */
+int ast_model_curve(ast_ctx* ctx, const double* params, double* vmod);
+
+typedef struct ast_fit_cfg {
+    uint64_t seed;          /* -seed; chains draw from Philox4x32-10 keyed by (seed, chain) */
+    int64_t  n_chains;      /* N_BLOCKS*BSIZE in the reference */
+    int32_t  group_size;    /* chains per result group (BSIZE); n_chains % group_size == 0 */
+    int32_t  n_stages;      /* -Nstages */
+    int32_t  reopt;         /* -reopt: start from params0 */
+    int32_t  precision;     /* AST_PREC_* */
+    int64_t  evals_cap;     /* per chain and stage, checked where N_STEPS is; 0 = none */
+    int32_t  steps_cap;     /* N_STEPS (asteroid.h:213); 0 = 5000 */
+    int32_t  tpb;           /* threads per CTA; 0 = autotuned */
+    const double* params0;  /* [n_params] start model for reopt (d_params0) */
+} ast_fit_cfg;
+
+typedef struct ast_fit_out {
+    double*  best_f;        /* [n_groups]            d_f          (may be NULL) */
+    double*  best_params;   /* [n_groups][n_params]  d_params     (may be NULL) */
+    double*  best_dv;       /* [n_groups][n_filters] d_dV         (may be NULL) */
+    double*  chain_f;       /* [n_chains] final best of every chain (may be NULL) */
+    int64_t  n_evals;       /* chi^2 evaluations performed */
+    int64_t  n_fits;        /* chains finished (all stages) */
+    double   kernel_ms;     /* device time of the simplex launches */
+} ast_fit_out;
+
+/* One full fitting pass: setup_kernel + chi2_gpu + the host argmin inputs
+ * (asteroid.c:626-759).  Group g's best follows the reference's block best: lowest chi^2,
+ * lowest chain index on ties; its delta_V is that chain's last evaluation's (cuda.c:1816-1821). */
+int ast_fit(ast_ctx* ctx, const ast_fit_cfg* cfg, ast_fit_out* out);
+
+/* The same pass split into resumable launches: chain state stays resident on the device
+ * between ast_fit_step calls.  Each step lets every chain slot perform at most
+ * evals_per_slot evaluations; *done becomes 1 when all stages of all chains finished. */
+int ast_fit_begin(ast_ctx* ctx, const ast_fit_cfg* cfg);
+int ast_fit_step(ast_ctx* ctx, int64_t evals_per_slot, int32_t* done, void* stream);
+int ast_fit_end(ast_ctx* ctx, ast_fit_out* out);
+
+/* Number of chain slots (persistent threads) the fit kernel of this context runs. */
+int64_t ast_fit_slots(ast_ctx* ctx);
+
+/* Device-side evaluation and fit counters since ast_fit_begin. */
+int ast_fit_counters(ast_ctx* ctx, int64_t* n_evals, int64_t* n_fits);
+
+/* The CUDA stream the context launches on (a cudaStream_t). */
+void* ast_stream(ast_ctx* ctx);
+
+/* Peak-rate probe: times an FP64 (kind 0) or FP32 (kind 1) FMA loop over every SM and
+ * returns GFLOP/s in *gflops.  Used as the roofline denominator for CUDA-core bound kernels. */
+int ast_probe_peak(int32_t device, int32_t kind, double* gflops);
+
+/* Library version string. */
+const char* ast_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ASTEROID_GB300_H */

@@ -1,0 +1,73 @@
+#!/usr/bin/env bash
+# build_ref.sh -- TEST INFRASTRUCTURE ONLY.  Builds the reference's own chi^2 code from its
+# sources, where they lie, into oracle/_ref/ (git-ignored):
+#
+#   libref_<variant>.so  host build of chi2one / x2params / params2x / ODE_func (cuda.c:13-1319)
+#                        with oracle/ref_harness_host.cu as entry points; used here to pin the
+#                        oracle and to generate tests/golden/.
+#   ref_<variant>.cubin  device build (sm_100) of the same functions plus
+#                        oracle/ref_harness_kernel.cu; loaded on the GPU by
+#                        oracle/ref_gpu_loader.cpp to check the CUDA path at 1e-12.
+#
+# The reference's asteroid.h and cuda.c are streamed through sed into nvcc's standard input:
+# the four device functions become __host__ __device__ (host build only), N_FILTERS becomes 8
+# and TIME_STEP the variant's step.  The variant macros are the reference's own (-DTORQUE ...).
+# Nothing of the reference is written to disk.  Needs the reference checkout (default
+# /root/reference, or $AST_REFERENCE_DIR); without it the script does nothing.
+set -euo pipefail
+here="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
+REF="${AST_REFERENCE_DIR:-/root/reference}"
+OUT="$here/_ref"
+if [[ ! -f "$REF/cuda.c" || ! -f "$REF/asteroid.h" ]]; then
+    echo "build_ref.sh: no reference checkout at $REF; skipping" >&2
+    exit 0
+fi
+mkdir -p "$OUT"
+
+# name  time_step  macros...
+VARIANTS=(
+  "ppsi_torque_acc 1e-2 -DP_PSI -DTORQUE -DACC"
+  "ppsi_torque_sp 1e-2 -DP_PSI -DTORQUE"
+  "torque_interp_acc 1e-2 -DTORQUE -DINTERP -DACC"
+  "bc_interp_acc 1e-2 -DBC -DINTERP -DACC"
+  "bw_torque_acc 1e-2 -DBW_BALL -DTORQUE -DACC"
+  "c2_nudge_acc 5e-3 -DP_PSI -DTORQUE -DINTERP -DACC -DNUDGE"
+  "bc_torque_ppsi_acc 1e-2 -DBC -DTORQUE -DP_PSI -DACC"
+  "free_acc 1e-2 -DACC"
+  "bc_interp_sp 1e-2 -DBC -DINTERP"
+)
+
+stream_source() {  # $1 = time step, $2 = 1 for the host build
+    local ts="$1" host="$2"
+    sed -e 's/^const int N_FILTERS = 1;/const int N_FILTERS = 8;/' \
+        -e "s/^const double TIME_STEP = 1e-2;.*/const double TIME_STEP = $ts;/" "$REF/asteroid.h"
+    if [[ "$host" == 1 ]]; then
+        sed -e 's/^#include "asteroid.h"//' \
+            -e 's/^__device__ void ODE_func/__host__ __device__ void ODE_func/' \
+            -e 's/^__device__ CHI_FLOAT chi2one/__host__ __device__ CHI_FLOAT chi2one/' \
+            -e 's/^__device__ void params2x/__host__ __device__ void params2x/' \
+            -e 's/^__device__ int x2params/__host__ __device__ int x2params/' "$REF/cuda.c"
+        cat "$here/ref_harness_host.cu"
+    else
+        sed -e 's/^#include "asteroid.h"//' "$REF/cuda.c"
+        cat "$here/ref_harness_kernel.cu"
+    fi
+}
+
+pids=()
+for v in "${VARIANTS[@]}"; do
+    read -r name ts macros <<<"$v"
+    if [[ "${1:-all}" == "all" || "${1:-all}" == "host" ]]; then
+        ( stream_source "$ts" 1 | nvcc -x cu -arch=sm_100 -O2 -DMAIN $macros -I"$REF" \
+              -Xcompiler -fPIC,-ffp-contract=off -shared -w -o "$OUT/libref_$name.so" - ) &
+        pids+=($!)
+    fi
+    if [[ -f "$here/ref_harness_kernel.cu" && ( "${1:-all}" == "all" || "${1:-all}" == "cubin" ) ]]; then
+        ( stream_source "$ts" 0 | nvcc -x cu -cubin -arch=sm_100 -O3 -DMAIN $macros -I"$REF" -w \
+              -o "$OUT/ref_$name.cubin" - ) &
+        pids+=($!)
+    fi
+done
+rc=0
+for p in "${pids[@]}"; do wait "$p" || rc=1; done
+exit $rc

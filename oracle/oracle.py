@@ -1,0 +1,210 @@
+"""THE ORACLE (Python side).  TEST INFRASTRUCTURE ONLY.
+
+ctypes access to oracle/_build/liboracle.so (the CPU restatement in chi2_oracle.c) and to the
+reference's own host build in oracle/_ref/libref_<variant>.so (oracle/build_ref.sh).  Only the
+tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "_build" / "liboracle.so"
+REF_DIR = HERE / "_ref"
+
+_lib = None
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            import sys
+            sys.path.insert(0, str(HERE.parent))
+            from asteroid_gb300 import build
+            build.build_oracle()
+        lib = C.CDLL(str(LIB_PATH))
+        V = C.c_void_p
+        lib.orc_chi2.restype = C.c_double
+        lib.orc_chi2.argtypes = [V, V, V, V]
+        lib.orc_chi2_batch.restype = None
+        lib.orc_chi2_batch.argtypes = [V, V, V, C.c_int64, V, V, C.c_int]
+        lib.orc_model_curve.restype = None
+        lib.orc_model_curve.argtypes = [V, V, V, V]
+        lib.orc_x2params.restype = C.c_int
+        lib.orc_x2params.argtypes = [V, C.c_int, V, V]
+        lib.orc_params2x.restype = None
+        lib.orc_params2x.argtypes = [V, V, V]
+        lib.orc_uniform.restype = C.c_float
+        lib.orc_uniform.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32]
+        lib.orc_philox4x32_10.restype = None
+        lib.orc_philox4x32_10.argtypes = [V, V, V]
+        lib.orc_max_threads.restype = C.c_int
+        lib.orc_fit.restype = None
+        lib.orc_fit.argtypes = [V, V, C.c_uint64, C.c_int64, C.c_int32, C.c_int32, C.c_int32, V, C.c_int64, C.c_int32,
+                                V, V, V, V, V]
+        _lib = lib
+    return _lib
+
+
+def _ptrs(model, obs):
+    """(model*, obs*) plus the objects that keep the ctypes structures alive."""
+    cobs = obs.as_c()
+    return C.cast(C.byref(model), C.c_void_p), C.cast(C.byref(cobs), C.c_void_p), cobs
+
+
+def chi2(model, obs, params):
+    lib = load()
+    mp, op, keep = _ptrs(model, obs)
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    dv = np.zeros(obs.n_filters)
+    r = lib.orc_chi2(mp, op, p.ctypes.data, dv.ctypes.data)
+    return r, dv
+
+
+def chi2_batch(model, obs, params, threads: int = 0):
+    lib = load()
+    mp, op, keep = _ptrs(model, obs)
+    p = np.ascontiguousarray(np.atleast_2d(params), dtype=np.float64)
+    n = p.shape[0]
+    out = np.zeros(n)
+    dv = np.zeros((n, obs.n_filters))
+    lib.orc_chi2_batch(mp, op, p.ctypes.data, n, out.ctypes.data, dv.ctypes.data, int(threads))
+    return out, dv
+
+
+def model_curve(model, obs, params):
+    lib = load()
+    mp, op, keep = _ptrs(model, obs)
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    out = np.zeros(obs.n_data)
+    lib.orc_model_curve(mp, op, p.ctypes.data, out.ctypes.data)
+    return out
+
+
+def x2params(model, x, reopt=1):
+    lib = load()
+    xx = np.ascontiguousarray(x, dtype=np.float64)
+    p = np.zeros(model.n_params)
+    rc = lib.orc_x2params(C.cast(C.byref(model), C.c_void_p), int(reopt), xx.ctypes.data, p.ctypes.data)
+    return None if rc else p
+
+
+def params2x(model, params):
+    lib = load()
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    x = np.zeros(model.n_params)
+    lib.orc_params2x(C.cast(C.byref(model), C.c_void_p), p.ctypes.data, x.ctypes.data)
+    return x
+
+
+def uniform(seed, chain, stage, k):
+    return load().orc_uniform(seed, chain, stage, k)
+
+
+def philox(ctr, key):
+    c = np.ascontiguousarray(ctr, dtype=np.uint32)
+    k = np.ascontiguousarray(key, dtype=np.uint32)
+    out = np.zeros(4, np.uint32)
+    load().orc_philox4x32_10(c.ctypes.data, k.ctypes.data, out.ctypes.data)
+    return out
+
+
+def fit(model, obs, seed, n_chains, group_size, n_stages=1, reopt=False, params0=None, evals_cap=0, steps_cap=0):
+    """Group/stage simplex driver on the CPU (small cases)."""
+    lib = load()
+    mp, op, keep = _ptrs(model, obs)
+    G = n_chains // group_size
+    bf = np.zeros(G)
+    bp = np.zeros((G, model.n_params))
+    bdv = np.zeros((G, obs.n_filters))
+    cf = np.zeros(n_chains)
+    ne = C.c_int64(0)
+    p0 = np.ascontiguousarray(params0 if params0 is not None else np.zeros(model.n_params), dtype=np.float64)
+    lib.orc_fit(mp, op, int(seed), int(n_chains), int(group_size), int(n_stages), int(bool(reopt)), p0.ctypes.data,
+                int(evals_cap), int(steps_cap), bf.ctypes.data, bp.ctypes.data, bdv.ctypes.data, cf.ctypes.data,
+                C.cast(C.byref(ne), C.c_void_p))
+    return {"best_f": bf, "best_params": bp, "best_dv": bdv, "chain_f": cf, "n_evals": ne.value}
+
+
+def max_threads() -> int:
+    return int(load().orc_max_threads())
+
+
+# ---------------------------------------------------------------- the reference's host build
+
+class RefHost:
+    """The reference's own chi2one / x2params / params2x, built from its sources."""
+
+    def __init__(self, variant: str):
+        path = REF_DIR / f"libref_{variant}.so"
+        if not path.exists():
+            raise FileNotFoundError(path)
+        lib = C.CDLL(str(path))
+        V = C.c_void_p
+        I = C.c_int
+        lib.refh_chi2.restype = I
+        lib.refh_chi2.argtypes = [V, I, V, I, V, I, I, I, V, V, V, V, V, V, V, V, V, I, V, V, V, V, V]
+        lib.refh_x2params.restype = I
+        lib.refh_x2params.argtypes = [V, I, V, I, V, I, C.c_float, C.c_float, I, V, V]
+        lib.refh_params2x.restype = I
+        lib.refh_params2x.argtypes = [V, I, V, I, V, I, V, V]
+        for n in ("refh_n_params", "refh_n_types", "refh_chi_float_bytes", "refh_max_filters"):
+            getattr(lib, n).restype = I
+        lib.refh_time_step.restype = C.c_double
+        self.lib = lib
+        self.n_params = lib.refh_n_params()
+        self.n_types = lib.refh_n_types()
+        self.time_step = lib.refh_time_step()
+
+    def _tables(self, m):
+        prop = np.ctypeslib.as_array(m.property).reshape(-1, 6)[: m.n_params].astype(np.int32).copy()
+        types = np.ctypeslib.as_array(m.types)[: m.n_types].astype(np.int32).copy()
+        lim = np.ctypeslib.as_array(m.limits).reshape(2, -1).astype(np.float64).copy()
+        return prop, types, lim
+
+    def chi2(self, m, obs, params):
+        prop, types, lim = self._tables(m)
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        out = np.zeros(1)
+        dv = np.zeros(max(obs.n_filters, 1))
+        cobs = obs  # arrays
+        rc = self.lib.refh_chi2(prop.ctypes.data, m.n_params, types.ctypes.data, m.n_types, lim.ctypes.data,
+                                lim.shape[1], obs.n_data, obs.n_filters, obs.mjd.ctypes.data, obs.v.ctypes.data,
+                                obs.w.ctypes.data, obs.filt.ctypes.data, obs.e_unit.ctypes.data,
+                                obs.s_unit.ctypes.data, np.ascontiguousarray(obs.eph_e).ctypes.data,
+                                np.ascontiguousarray(obs.eph_s).ctypes.data,
+                                np.ascontiguousarray(obs.eph_mjd0).ctypes.data, int(obs.t_min.size),
+                                obs.t_min.ctypes.data, obs.v_min.ctypes.data, p.ctypes.data, out.ctypes.data,
+                                dv.ctypes.data)
+        del cobs
+        if rc:
+            raise RuntimeError(f"refh_chi2 failed ({rc}): tables do not match the reference build")
+        return out[0], dv
+
+    def x2params(self, m, x, reopt=1):
+        prop, types, lim = self._tables(m)
+        xx = np.ascontiguousarray(x, dtype=np.float64)
+        p = np.zeros(m.n_params)
+        rc = self.lib.refh_x2params(prop.ctypes.data, m.n_params, types.ctypes.data, m.n_types, lim.ctypes.data,
+                                    lim.shape[1], m.ppsi1, m.ppsi2, int(reopt), xx.ctypes.data, p.ctypes.data)
+        if rc < 0:
+            raise RuntimeError("refh_x2params: tables do not match the reference build")
+        return None if rc else p
+
+    def params2x(self, m, params):
+        prop, types, lim = self._tables(m)
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        x = np.zeros(m.n_params)
+        rc = self.lib.refh_params2x(prop.ctypes.data, m.n_params, types.ctypes.data, m.n_types, lim.ctypes.data,
+                                    lim.shape[1], p.ctypes.data, x.ctypes.data)
+        if rc:
+            raise RuntimeError("refh_params2x: tables do not match the reference build")
+        return x

@@ -1,0 +1,97 @@
+"""chi^2 batch evaluation on the GPU (FP64 plain path) against the oracle.
+
+Tolerances: the oracle is compiled without fused multiply-adds and with the host libm, the
+kernel with nvcc's contractions and CUDA's libm, so results differ by rounding only.  For
+parameter vectors whose rotation the fixed-step RK4 resolves (h * L <= 0.5) the relative chi^2
+difference is bounded by RTOL_FP64; under-resolved vectors (RK4 unstable, chaotic in the last
+bit) are compared for agreement on finiteness only.  The 1e-12 bar is against the reference's
+own kernel (tests/test_ref_kernel.py), which shares the compiler and libm.
+"""
+import numpy as np
+import pytest
+
+from asteroid_gb300 import api
+
+pytestmark = pytest.mark.gpu
+
+RTOL_FP64 = 1e-9
+
+
+def _vectors(model, n, seed, reopt=0, resolved=True):
+    rng = np.random.default_rng(seed)
+    names = api.param_names(model)
+    iL = names.index("L")
+    out = []
+    while len(out) < n:
+        x = rng.uniform(0, 1, model.n_params)
+        p = api.x2params(model, x, reopt=reopt)
+        if p is None:
+            continue
+        if resolved and not p[iL] * model.time_step <= 0.5:
+            continue
+        out.append(p)
+    return np.array(out)
+
+
+@pytest.mark.parametrize("name", ["c0acc", "c1", "c1bc", "c2"])
+def test_fp64_matches_oracle(gpu, oracle_mod, synth_objects, name):
+    s = synth_objects(name)
+    P = _vectors(s.model, 200, seed=3)
+    P = np.vstack([P, s.params_true[None, :]])
+    with api.Engine(s.model, s.obs) as eng:
+        chi2, dv = eng.eval(P)
+    ref, ref_dv = oracle_mod.chi2_batch(s.model, s.obs, P)
+    both_nan = np.isnan(chi2) & np.isnan(ref)
+    ok = ~both_nan
+    assert np.all(np.isfinite(chi2[ok]) == np.isfinite(ref[ok]))
+    fin = ok & np.isfinite(ref)
+    acc = bool(s.model.flags & api.ACC)
+    rtol = RTOL_FP64 if acc else 2e-6  # without ACC chi2 is rounded to float (CHI_FLOAT)
+    if s.model.flags & api.NUDGE:
+        rtol = max(rtol, 5e-6)  # the NUDGE merit is float arithmetic with powf
+    rel = np.abs(chi2[fin] - ref[fin]) / np.maximum(np.abs(ref[fin]), 1e-300)
+    assert rel.max() <= rtol, f"max rel chi2 diff {rel.max():.3e}"
+    dvrel = np.abs(dv[fin] - ref_dv[fin]) / np.maximum(np.abs(ref_dv[fin]), 1e-12)
+    assert dvrel.max() <= max(rtol, 1e-9)
+
+
+def test_true_model_chi2_near_one(gpu, synth_objects):
+    """The generating model fits its own noisy data: reduced chi^2 ~ 1 (sigma = 0.1)."""
+    s = synth_objects("c0acc")
+    with api.Engine(s.model, s.obs) as eng:
+        chi2, dv = eng.eval(s.params_true[None, :])
+    assert 0.7 < chi2[0] < 1.4
+    assert abs(dv[0, 0] - s.dv_true[0]) < 0.05
+
+
+def test_model_curve_matches_oracle(gpu, oracle_mod, synth_objects):
+    s = synth_objects("c1")
+    with api.Engine(s.model, s.obs) as eng:
+        v = eng.model_curve(s.params_true)
+    ref = oracle_mod.model_curve(s.model, s.obs, s.params_true)
+    assert np.max(np.abs(v - ref)) < 1e-9
+
+
+def test_unresolved_vectors_agree_on_finiteness(gpu, oracle_mod, synth_objects):
+    s = synth_objects("c0acc")
+    P = _vectors(s.model, 100, seed=9, reopt=1, resolved=False)
+    with api.Engine(s.model, s.obs) as eng:
+        chi2, _ = eng.eval(P)
+    ref, _ = oracle_mod.chi2_batch(s.model, s.obs, P)
+    # Vectors whose RK4 diverges to NaN on one side diverge on the other too, almost always.
+    agree = np.mean(np.isnan(chi2) == np.isnan(ref))
+    assert agree > 0.9
+
+
+def test_eval_rejects_bad_precision(gpu, synth_objects):
+    s = synth_objects("c0acc")
+    with api.Engine(s.model, s.obs) as eng:
+        with pytest.raises(Exception):
+            eng.eval(s.params_true[None, :], precision=7)
+
+
+def test_empty_batch(gpu, synth_objects):
+    s = synth_objects("c0acc")
+    with api.Engine(s.model, s.obs) as eng:
+        chi2, dv = eng.eval(np.zeros((0, s.model.n_params)))
+    assert chi2.shape == (0,)
