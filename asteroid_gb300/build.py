@@ -23,8 +23,8 @@ ORACLE_BUILD = ORACLE / "_build"
 ARCH = os.environ.get("AST_CUDA_ARCH", "sm_103a")
 GENCODE = [f"-gencode=arch=compute_{ARCH[3:]},code={ARCH}"]
 CU_SOURCES = ["csrc/engine.cu", "csrc/fit.cu"]
-C_SOURCES = ["host/tables.c", "host/read_data.c", "host/errors.c"]
-CLI_SOURCES = ["host/asteroid.c", "host/misc.c"]
+C_SOURCES = ["host/tables.c", "host/read_data.c", "host/misc.c", "host/errors.c"]
+CLI_SOURCES = ["host/asteroid.c"]
 
 
 def _nvcc() -> str:
@@ -108,6 +108,15 @@ def build_oracle(force: bool = False) -> Path:
     if force or _stale(lib, deps):
         _run(["gcc", "-O2", "-fPIC", "-shared", "-std=c11", "-ffp-contract=off", "-fopenmp", f"-I{INCLUDE}",
               str(src), "-o", str(lib), "-lm"])
+    # Driver-API loader for the reference kernel cubins (oracle/_ref/ref_*.cubin).
+    loader_src = ORACLE / "ref_gpu_loader.cpp"
+    loader = ORACLE_BUILD / "libref_gpu_loader.so"
+    if loader_src.exists() and (force or _stale(loader, [loader_src])):
+        cuda = Path(_nvcc()).resolve().parent.parent
+        libdirs = [p for p in (cuda / "lib64" / "stubs", cuda / "lib64", cuda / "targets" / "sbsa-linux" / "lib" / "stubs")
+                   if p.exists()]
+        _run(["g++", "-O2", "-fPIC", "-shared", "-std=c++17", f"-I{cuda / 'include'}", str(loader_src), "-o", str(loader),
+              *[f"-L{d}" for d in libdirs], "-lcuda"])
     return lib
 
 

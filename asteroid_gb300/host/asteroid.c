@@ -1,0 +1,248 @@
+/*
+ * asteroid.c -- command-line driver (host, C), the drop-in for the reference's asteroid
+ * binary on its fitting path (asteroid.c:18-831 of the reference).
+ *
+ * Same switches and meanings: -i -o -m -t -reopt -keep -best -seed -N -Nstages -f -l -Ppsi
+ * (asteroid.c:173-431), same output line ("%13.6e " chi^2, "%13.6e " per-filter delta_V,
+ * "%15.11f " parameters in Property order, asteroid.c:798-811), same stdout best line
+ * (asteroid.c:770-779), same keep/best/travel semantics (asteroid.c:741-818).  Periodic
+ * parameters are printed unwrapped, as the reference does (its wrap loop never runs, see
+ * asteroid.c:753).
+ *
+ * The reference fixes the model variant, N_BLOCKS, BSIZE and TIME_STEP at compile time; here
+ * the compile-time macros (-DTORQUE -DBC -DBW_BALL -DP_PSI -DACC -DNUDGE -DINTERP, -DN_BLOCKS,
+ * -DBSIZE, -DTIME_STEP) give the defaults and these extra switches override them at run time:
+ *   -variant TORQUE,P_PSI,...   -Nblocks n   -bsize n   -time_step h   -mixed   -evals n
+ *   -eph dir (directory of asteroid.eph / earth.eph / sun.eph, default ".")
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+#include "asteroid_gb300.h"
+
+#ifndef N_BLOCKS
+#define N_BLOCKS 152
+#endif
+#ifndef BSIZE
+#define BSIZE 256
+#endif
+#ifndef TIME_STEP
+#define TIME_STEP 1e-2
+#endif
+
+static int default_flags(void)
+{
+    int f = 0;
+#ifdef TORQUE
+    f |= AST_TORQUE;
+#endif
+#ifdef BC
+    f |= AST_BC;
+#endif
+#ifdef BW_BALL
+    f |= AST_BW_BALL;
+#endif
+#ifdef P_PSI
+    f |= AST_P_PSI;
+#endif
+#ifdef INTERP
+    f |= AST_INTERP;
+#endif
+#ifdef ACC
+    f |= AST_ACC;
+#endif
+#ifdef NUDGE
+    f |= AST_NUDGE;
+#endif
+    if (f == 0) f = AST_TORQUE | AST_P_PSI; /* the README's fiducial model */
+    return f;
+}
+
+static int parse_variant(const char* s)
+{
+    static const struct { const char* n; int f; } names[] = {
+        {"TORQUE", AST_TORQUE}, {"BC", AST_BC}, {"BW_BALL", AST_BW_BALL}, {"P_PSI", AST_P_PSI},
+        {"INTERP", AST_INTERP}, {"ACC", AST_ACC}, {"NUDGE", AST_NUDGE}, {"LS", 0}};
+    int f = 0;
+    char buf[256];
+    snprintf(buf, sizeof(buf), "%s", s);
+    for (char* tok = strtok(buf, ",+ "); tok; tok = strtok(NULL, ",+ ")) {
+        if (tok[0] == '-' && tok[1] == 'D') tok += 2;
+        int found = 0;
+        for (size_t k = 0; k < sizeof(names) / sizeof(names[0]); k++)
+            if (strcmp(tok, names[k].n) == 0) { f |= names[k].f; found = 1; }
+        if (!found) { fprintf(stderr, "Unknown variant %s\n", tok); exit(1); }
+    }
+    return f;
+}
+
+static void usage(void)
+{
+    printf("\n Command line arguments:\n\n");
+    printf("-best : only keep the best result\n");
+    printf("-f type_constant value: forces the parameter with the type_constant to be frozen during optimization at \"value\" \n");
+    printf("-i name : input (data) file name\n");
+    printf("-keep : keep all intermediate results, not just the best ones\n");
+    printf("-l type_constant limit1 limit2 : specify range for the parameter type_constant\n");
+    printf("-m param1 param2 ... paramN : input model parameters, for plotting and re-optimization\n");
+    printf("     If one of the parameters has a special value of \"v\", it is allowed to vary randomly within its full range.\n");
+    printf("-N number : exit after \"number\" cycles\n");
+    printf("-Nstages number : each initial optimization stage is followed by \"number-1\" reoptimization stages\n");
+    printf("-o name : output (results) file name\n");
+    printf("-Ppsi min max : minimum and maximum values for Ppsi period, in hours\n");
+    printf("-reopt : reoptimize the model provided with -m switch\n");
+    printf("-seed SEED : use the SEED number to initialize the random number generator\n");
+    printf("-t : travelling reoptimization\n");
+    printf("\n GB300 engine switches: -variant TORQUE,P_PSI,... -Nblocks n -bsize n -time_step h -mixed -evals n -eph dir\n\n");
+}
+
+int main(int argc, char** argv)
+{
+    if (argc == 1) { usage(); return 0; }
+    int flags = default_flags();
+    int n_blocks = N_BLOCKS, bsize = BSIZE, precision = AST_PREC_FP64;
+    double time_step = TIME_STEP, ppsi1 = 2.0, ppsi2 = 4800.0;
+    long long evals_cap = 0;
+    const char *in = NULL, *outp = NULL, *eph = ".";
+    int travel = 0, keep = 0, best = 0, reopt = 0, model_given = 0, plot = 0, Ncases = -1, Nstages = 1;
+    unsigned long seed = 0;
+    int n_frozen = 0, n_limits = 0;
+    int Fi[64], Li[64];
+    double Fv[64], L0[64], L1[64];
+    char* mtok[AST_MAX_PARAMS + 2] = {0};
+    int mtok_n = 0;
+
+    for (int j = 1; j < argc;) {
+        const char* a = argv[j];
+        if (a[0] != '-') { printf("Bad arguments!\n"); return 1; }
+#define NEED(k) do { if (j + (k) >= argc) { printf("Bad arguments!\n"); return 1; } } while (0)
+        if (!strcmp(a, "-i")) { NEED(1); in = argv[j + 1]; j += 2; }
+        else if (!strcmp(a, "-o")) { NEED(1); outp = argv[j + 1]; j += 2; }
+        else if (!strcmp(a, "-Ppsi")) { NEED(2); ppsi1 = atof(argv[j + 1]); ppsi2 = atof(argv[j + 2]); j += 3; }
+        else if (!strcmp(a, "-m")) {
+            /* The parameter count depends on the variant, which may come later: keep the tokens. */
+            j++;
+            while (j < argc && mtok_n < AST_MAX_PARAMS && (argv[j][0] != '-' || (argv[j][1] >= '0' && argv[j][1] <= '9') || argv[j][1] == '.'))
+                mtok[mtok_n++] = argv[j++];
+            model_given = 1;
+        }
+        else if (!strcmp(a, "-plot")) { plot = 1; j++; }
+        else if (!strcmp(a, "-t")) { travel = 1; j++; }
+        else if (!strcmp(a, "-reopt")) { reopt = 1; j++; }
+        else if (!strcmp(a, "-keep")) { keep = 1; j++; }
+        else if (!strcmp(a, "-best")) { best = 1; j++; }
+        else if (!strcmp(a, "-seed")) { NEED(1); seed = strtoul(argv[j + 1], NULL, 10); j += 2; }
+        else if (!strcmp(a, "-N")) { NEED(1); Ncases = atoi(argv[j + 1]); j += 2; }
+        else if (!strcmp(a, "-Nstages")) { NEED(1); Nstages = atoi(argv[j + 1]); j += 2; }
+        else if (!strcmp(a, "-f")) { NEED(2); if (n_frozen < 64) { Fi[n_frozen] = atoi(argv[j + 1]); Fv[n_frozen++] = atof(argv[j + 2]); } j += 3; }
+        else if (!strcmp(a, "-l")) { NEED(3); if (n_limits < 64) { Li[n_limits] = atoi(argv[j + 1]); L0[n_limits] = atof(argv[j + 2]); L1[n_limits++] = atof(argv[j + 3]); } j += 4; }
+        else if (!strcmp(a, "-variant")) { NEED(1); flags = parse_variant(argv[j + 1]); j += 2; }
+        else if (!strcmp(a, "-Nblocks")) { NEED(1); n_blocks = atoi(argv[j + 1]); j += 2; }
+        else if (!strcmp(a, "-bsize")) { NEED(1); bsize = atoi(argv[j + 1]); j += 2; }
+        else if (!strcmp(a, "-time_step")) { NEED(1); time_step = atof(argv[j + 1]); j += 2; }
+        else if (!strcmp(a, "-mixed")) { precision = AST_PREC_MIXED; j++; }
+        else if (!strcmp(a, "-evals")) { NEED(1); evals_cap = atoll(argv[j + 1]); j += 2; }
+        else if (!strcmp(a, "-eph")) { NEED(1); eph = argv[j + 1]; j += 2; }
+        else { printf("Bad arguments!\n"); return 1; }
+#undef NEED
+    }
+    if (!in) { printf("-i parameter is missing!\n"); return 1; }
+    if ((reopt || plot) && !model_given) { printf("-reopt and -plot switches require -m switch!\n"); return 1; }
+    if (!reopt && !plot && model_given) { printf("-m can only be used together with -reopt or -plot switches!\n"); return 1; }
+    if (plot) { printf("-plot is not part of this build's fitting path\n"); return 1; }
+
+    ast_model model;
+    if (ast_model_init(&model, flags, time_step, ppsi1, ppsi2)) { fprintf(stderr, "%s\n", ast_last_error()); return 1; }
+    const int N = model.n_params;
+    double params[AST_MAX_PARAMS] = {0};
+    if (model_given) {
+        if (mtok_n < N) { printf("Not enough of model parameters in -m switch!\n"); return 1; }
+        for (int k = 0; k < N; k++) {
+            if (mtok[k][0] == 'v') { ast_model_set_free_random(&model, k); params[k] = 0; }
+            else params[k] = atof(mtok[k]);
+        }
+    }
+    for (int k = 0; k < n_frozen; k++)
+        if (ast_model_freeze(&model, Fi[k], Fv[k])) { fprintf(stderr, "%s\n", ast_last_error()); return 1; }
+    for (int k = 0; k < n_limits; k++)
+        if (ast_model_set_limits(&model, Li[k], L0[k], L1[k])) { fprintf(stderr, "%s\n", ast_last_error()); return 1; }
+
+    ast_host_data* hd = NULL;
+    if (ast_read_data(in, eph, (flags & AST_INTERP) != 0, AST_MAX_FILTERS, &hd)) { printf("%s\n", ast_last_error()); return 1; }
+    printf("Filters:\n");
+    for (int k = 0; k < hd->obs.n_filters; k++) printf("%d: %c\n", k + 1, hd->filters[k]);
+    if (flags & AST_NUDGE) {
+        if (ast_read_minima("observed.min", hd)) { printf("%s\n", ast_last_error()); return 1; }
+        printf("%d minima in observed.min\n", hd->obs.n_minima);
+    }
+    ast_ctx* ctx = NULL;
+    if (ast_prepare(&model, &hd->obs, -1, &ctx)) { printf("%s\n", ast_last_error()); return 1; }
+    if (!outp) { printf("Bad output file name!\n"); return 1; }
+    const int NF = hd->obs.n_filters;
+    const long long n_chains = (long long)n_blocks * bsize;
+    printf("\n*** Simplex optimization ***\n\n");
+    printf("  N_threads = %lld\n", n_chains);
+    if (seed == 0) seed = (unsigned long)time(NULL);
+
+    double* h_f = (double*)malloc(sizeof(double) * n_blocks);
+    double* h_p = (double*)malloc(sizeof(double) * n_blocks * N);
+    double* h_dv = (double*)malloc(sizeof(double) * n_blocks * NF);
+    double* c_f = (double*)malloc(sizeof(double) * n_blocks);
+    double* c_p = (double*)malloc(sizeof(double) * n_blocks * N);
+    double* c_dv = (double*)malloc(sizeof(double) * n_blocks * NF);
+    for (int b = 0; b < n_blocks; b++) h_f[b] = 1e30;
+    int loop_counter = 0;
+    while (1) {
+        loop_counter++;
+        ast_fit_cfg cfg;
+        memset(&cfg, 0, sizeof(cfg));
+        /* The reference's cuRAND states advance across loops; here every loop has its own key. */
+        cfg.seed = (unsigned long long)seed + 0x9E3779B97F4A7C15ull * (unsigned long long)(loop_counter - 1);
+        cfg.n_chains = n_chains;
+        cfg.group_size = bsize;
+        cfg.n_stages = Nstages;
+        cfg.reopt = reopt;
+        cfg.precision = precision;
+        cfg.evals_cap = evals_cap;
+        cfg.params0 = params;
+        ast_fit_out out;
+        memset(&out, 0, sizeof(out));
+        out.best_f = c_f;
+        out.best_params = c_p;
+        out.best_dv = c_dv;
+        if (ast_fit(ctx, &cfg, &out)) { printf("%s\n", ast_last_error()); return 1; }
+        /* d_f keeps each block's best across loops unless -keep resets it (asteroid.c:816-818). */
+        for (int b = 0; b < n_blocks; b++)
+            if (c_f[b] < h_f[b]) {
+                h_f[b] = c_f[b];
+                memcpy(h_p + (size_t)b * N, c_p + (size_t)b * N, sizeof(double) * N);
+                memcpy(h_dv + (size_t)b * NF, c_dv + (size_t)b * NF, sizeof(double) * NF);
+            }
+        int i_best = 0;
+        double chi2_tot = 1e32;
+        for (int b = 0; b < n_blocks; b++)
+            if (h_f[b] < chi2_tot) { chi2_tot = h_f[b]; i_best = b; }
+        if (reopt && travel) memcpy(params, h_p + (size_t)i_best * N, sizeof(double) * N);
+        printf("%13.6e ", h_f[i_best]);
+        for (int k = 0; k < N; k++) printf("%15.11f ", h_p[(size_t)i_best * N + k]);
+        printf("\n");
+        fflush(stdout);
+        FILE* fp = fopen(outp, keep ? "a" : "w");
+        if (!fp) { printf("Bad output file name!\n"); return 1; }
+        int i1 = best ? i_best : 0, i2 = best ? i_best + 1 : n_blocks;
+        char line[8192];
+        for (int b = i1; b < i2; b++) {
+            ast_format_result(line, sizeof(line), h_f[b], h_dv + (size_t)b * NF, NF, h_p + (size_t)b * N, N);
+            fputs(line, fp);
+        }
+        fclose(fp);
+        if (keep)
+            for (int b = 0; b < n_blocks; b++) h_f[b] = 1e30;
+        if (loop_counter == Ncases) break;
+    }
+    ast_destroy(ctx);
+    ast_free_host_data(hd);
+    free(h_f); free(h_p); free(h_dv); free(c_f); free(c_p); free(c_dv);
+    return 0;
+}

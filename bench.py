@@ -1,0 +1,360 @@
+"""Benchmark: chi^2 evaluations/s of the fitting hot path on one GB300 (config 2 by default).
+
+Workload (config 2 of the benchmark set): a 2000-point, 3-filter light curve over 60 days with
+INTERP ephemerides, TORQUE + P_PSI + ACC + NUDGE, TIME_STEP 5e-3, fitted by 65536 random-start
+simplex chains of 20000 chi^2 evaluations each.  The full job (1.3e9 evaluations) takes far
+longer than a benchmark may run, so a "step" is one resumable launch of the persistent simplex
+kernel in which every chain slot performs a fixed number of evaluations at full per-evaluation
+cost; `value` is the evaluations of the timed steps over their device time.
+
+Keys beyond the driver's contract:
+  fp64        the plain FP64 path on the same workload (evals/s) and mixed/fp64 speed-up
+  accuracy    |dchi2|/chi2 of the mixed path against the FP64 path on sampled vectors
+  roofline    algorithmic flops per evaluation x evals/s against the measured FMA peak
+  cpu_baseline  the oracle port on the host cores (bounded sample)
+  e2e         chi^2 evals/s through ast_eval_batch with host buffers (copies included)
+
+--impl reference times the CPU implementation of the path (the oracle port of the reference's
+chi2one; the reference's own host build is x86-only and does not run on the Arm host) on all
+host cores, same metric and workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "chi2_evals_per_s"
+UNIT = "evals/s"
+
+
+def rk4_steps(obs, time_step):
+    return int(np.sum(np.floor(np.diff(obs.mjd) / time_step + 1)))
+
+
+def algorithmic_flops(obs, model):
+    """Per-evaluation flops counted from the reference source (add/mul/div/sqrt = 1, fma = 2):
+    152 per RK4 step (4 right-hand sides of 18 + 80 for the stage combinations), 156 per
+    observation for the LS brightness and the filter sums, 6 per filter, 50 per-evaluation set-up.
+    Transcendental calls are not counted as flops (16 per RK4 step, 14 per observation)."""
+    n_rk4 = rk4_steps(obs, model.time_step)
+    return 152 * n_rk4 + 156 * obs.n_data + 6 * obs.n_filters + 50, 16 * n_rk4 + 14 * obs.n_data
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, gpu_index):
+        self.samples = []
+        self.proc = None
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[3 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+
+    t = torch.tensor([float(v)], device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+
+    t = torch.tensor([float(v)], device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def make_workload(args, tmp):
+    from asteroid_gb300 import synth
+
+    return synth.generate(args.config, tmp)
+
+
+def sample_vectors(model, n, seed, reopt=0):
+    from asteroid_gb300 import api
+
+    rng = np.random.default_rng(seed)
+    iL = api.param_names(model).index("L")
+    out = []
+    while len(out) < n:
+        p = api.x2params(model, rng.uniform(0, 1, model.n_params), reopt=reopt)
+        if p is not None and p[iL] * model.time_step <= 0.5:
+            out.append(p)
+    return np.array(out)
+
+
+def cpu_baseline(model, obs, seconds=15.0):
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+
+    from asteroid_gb300 import build
+
+    build.build_oracle()
+    threads = O.max_threads()
+    P = sample_vectors(model, 8 * threads, seed=99)
+    t0 = time.perf_counter()
+    O.chi2_batch(model, obs, P[: threads], threads=threads)  # warm
+    per = (time.perf_counter() - t0) / 1.0
+    n = max(threads, int(seconds / max(per, 1e-6) * threads))
+    P = sample_vectors(model, n, seed=100)
+    t0 = time.perf_counter()
+    O.chi2_batch(model, obs, P, threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n} parameter vectors of the workload's object, oracle chi2one restatement, OpenMP"}
+
+
+def run_fit_steps(eng, precision, n_chains, group, evals_cap, budget, warmup, steps, seed, stream_events):
+    """Warm-up + timed resumable launches; returns (evals, ms, fits, launches)."""
+    eng.fit_begin(n_chains=n_chains, group_size=group, seed=seed, precision=precision, evals_cap=evals_cap)
+    for _ in range(warmup):
+        eng.fit_step(budget)
+    e0, f0 = eng.fit_counters()
+    ms, launches = stream_events(lambda: [eng.fit_step(budget) for _ in range(steps)])
+    e1, f1 = eng.fit_counters()
+    eng.fit_end()
+    return e1 - e0, ms, f1 - f0, steps
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c2")
+    ap.add_argument("--chains", type=int, default=65536)
+    ap.add_argument("--evals-cap", type=int, default=20000)
+    ap.add_argument("--budget-mixed", type=int, default=0, help="evaluations per slot per step (0 = auto)")
+    ap.add_argument("--budget-fp64", type=int, default=0)
+    ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    args = ap.parse_args()
+
+    world, rank, local, dist = dist_setup()
+    tmp = tempfile.mkdtemp(prefix="astbench_")
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        from asteroid_gb300 import api, build, synth
+
+        build.build_engine()
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle as O
+
+        s = synth.generate(args.config, tmp, vmod_fn=lambda m, o, p: O.model_curve(m, o, p))
+        build.build_oracle()
+        threads = O.max_threads()
+        P = sample_vectors(s.model, threads, seed=5)
+        O.chi2_batch(s.model, s.obs, P, threads=threads)
+        for _ in range(args.warmup):
+            O.chi2_batch(s.model, s.obs, P, threads=threads)
+        t0 = time.perf_counter()
+        O.chi2_batch(s.model, s.obs, P, threads=threads)
+        per_step = 10.0
+        n = max(threads, int(per_step / max(time.perf_counter() - t0, 1e-6) * threads))
+        P = sample_vectors(s.model, n, seed=6)
+        times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            O.chi2_batch(s.model, s.obs, P, threads=threads)
+            times.append(time.perf_counter() - t0)
+        v = n * args.steps / sum(times)
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": {"workload": f"{args.config}: chi2one on {n} parameter vectors per step"},
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                                 "sample": f"{n} vectors per step; the reference's host build is x86-only, so the "
+                                           f"oracle port of its chi2one runs on this host"},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+
+    from asteroid_gb300 import api, build
+
+    build.build_engine()
+    torch.cuda.set_device(local)
+    s = make_workload(args, tmp)
+    model, obs = s.model, s.obs
+    eng = api.Engine(model, obs, device=local)
+    stream = torch.cuda.ExternalStream(eng.stream)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")
+
+    def timed(fn):
+        """Run fn between two events on the engine's stream, L2 flushed first; returns (ms, out)."""
+        barrier(dist)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        out = fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        barrier(dist)
+        return a.elapsed_time(b), out
+
+    n_rk4 = rk4_steps(obs, model.time_step)
+    flops, trans = algorithmic_flops(obs, model)
+    seed = 1234 + 7919 * rank
+
+    # Budgets: about one second of device time per step at the expected rates.
+    slots_guess = 152 * 256
+    b_mixed = args.budget_mixed or max(1, int(1.0 * 2.0e6 / slots_guess * 1.0e4 / max(n_rk4, 1)))
+    b_fp64 = args.budget_fp64 or max(1, int(1.0 * 1.5e5 / slots_guess * 1.25e4 / max(n_rk4, 1)))
+
+    with Clocks(local) as clk:
+        ev_m, ms_m, fits_m, launches_m = run_fit_steps(eng, api.PREC_MIXED, args.chains, 256, args.evals_cap, b_mixed,
+                                                       args.warmup, args.steps, seed, timed)
+    ms_m = max_over_ranks(dist, ms_m)
+    ev_m_all = sum_over_ranks(dist, ev_m)
+    value = ev_m_all / (ms_m * 1e-3)
+
+    fp64 = None
+    if not args.skip_fp64:
+        ev_d, ms_d, _, _ = run_fit_steps(eng, api.PREC_FP64, args.chains, 256, args.evals_cap, b_fp64,
+                                         max(1, args.warmup // 2 + 1), max(2, args.steps // 2), seed, timed)
+        ms_d = max_over_ranks(dist, ms_d)
+        fp64 = sum_over_ranks(dist, ev_d) / (ms_d * 1e-3)
+
+    # Accuracy of the mixed path against FP64 on sampled vectors and on the truth.
+    P = np.vstack([sample_vectors(model, 2047, seed=11 + rank), s.params_true[None, :]])
+    c64, _ = eng.eval(P, api.PREC_FP64)
+    c32, _ = eng.eval(P, api.PREC_MIXED)
+    ok = np.isfinite(c64) & (c64 < 1e29)
+    rel = np.abs(c32[ok] - c64[ok]) / np.abs(c64[ok])
+
+    # End to end through the C ABI with host buffers: ast_eval_batch, copies included.
+    B = 16384
+    Pe = sample_vectors(model, B, seed=21 + rank)
+    eng.eval(Pe[:256], api.PREC_MIXED)
+    t0 = time.perf_counter()
+    e2e_steps = 2
+    for _ in range(e2e_steps):
+        eng.eval(Pe, api.PREC_MIXED)
+    e2e_dt = max_over_ranks(dist, time.perf_counter() - t0)
+    e2e = sum_over_ranks(dist, B * e2e_steps) / e2e_dt
+
+    peak32 = api.probe_peak("fp32", local)
+    peak64 = api.probe_peak("fp64", local)
+    achieved = flops * value / 1e9 / max(world, 1)
+    cpu = cpu_baseline(model, obs, args.cpu_seconds) if (rank == 0 and world == 1) else None
+    clocks = clk.summary()
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_m / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 rhs/brightness + f64 state (mixed)", "data": "synthetic",
+            "config": {"workload": f"{args.config}: {obs.n_data} points, {obs.n_filters} filters, "
+                                   f"{api.flag_names(model.flags)}, TIME_STEP {model.time_step}, "
+                                   f"{args.chains} chains x {args.evals_cap} evals; timed slice of "
+                                   f"{b_mixed} evals/slot/step", "chains_per_gpu": args.chains,
+                       "n_data": obs.n_data, "rk4_steps_per_eval": n_rk4, "parallelism": f"replicas x{world}",
+                       "l2": "flushed before every timed region (256 MB write); simplex state ~100 MB, obs in smem"},
+            "fits_per_s": value / args.evals_cap,
+            "fp64": {"value": fp64, "unit": UNIT, "speedup_mixed_over_fp64": (value / fp64) if fp64 else None},
+            "accuracy": {"vectors": int(ok.sum()), "median_rel_dchi2": float(np.median(rel)),
+                         "p99_rel_dchi2": float(np.quantile(rel, 0.99)), "max_rel_dchi2": float(rel.max()),
+                         "frac_le_1e-6": float(np.mean(rel <= 1e-6))},
+            "roofline": {"bound": "fp32-pipe (CUDA cores)", "achieved": achieved, "peak": peak32 / 1e3 * 1e3,
+                         "unit": "GFLOP/s", "frac": achieved / peak32, "traffic": None,
+                         "flops_per_eval": flops, "transcendentals_per_eval": trans,
+                         "peak_source": "measured in this run by ast_probe_peak (FP32 FMA loop over every SM)",
+                         "fp64_peak_gflops": peak64},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": B * model.n_params * 8,
+                    "d2h_bytes_per_step": B * (1 + obs.n_filters) * 8, "path": "ast_eval_batch, mixed, host buffers"},
+            "gpu_launches": launches_m,
+            "clocks": clocks,
+        }
+        print(json.dumps(line))
+    eng.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -208,3 +208,37 @@ class RefHost:
         if rc:
             raise RuntimeError("refh_params2x: tables do not match the reference build")
         return x
+
+
+class RefKernel:
+    """The reference's own chi2one on the GPU (oracle/_ref/ref_<variant>.cubin, sm_100)."""
+
+    def __init__(self, variant: str):
+        self.cubin = REF_DIR / f"ref_{variant}.cubin"
+        if not self.cubin.exists():
+            raise FileNotFoundError(self.cubin)
+        lib = C.CDLL(str(HERE / "_build" / "libref_gpu_loader.so"))
+        lib.refk_eval_batch.restype = C.c_int
+        lib.refk_last_error.restype = C.c_char_p
+        self.lib = lib
+
+    def chi2_batch(self, model, obs, params):
+        from asteroid_gb300 import capi
+        P = np.ascontiguousarray(np.atleast_2d(params), dtype=np.float64)
+        n = P.shape[0]
+        types = np.ctypeslib.as_array(model.types)[: model.n_types].astype(np.int32).copy()
+        eph = np.concatenate([np.asarray(obs.eph_e).ravel(), np.asarray(obs.eph_s).ravel(),
+                              np.asarray(obs.eph_mjd0).ravel()]).astype(np.float64)
+        obs_bytes = 24 if model.flags & capi.INTERP else 72
+        chi2 = np.zeros(n)
+        dv = np.zeros((n, obs.n_filters))
+        V = C.c_void_p
+        rc = self.lib.refk_eval_batch(
+            str(self.cubin).encode(), obs_bytes, model.n_params, V(P.ctypes.data), n, V(types.ctypes.data),
+            model.n_types, obs.n_data, obs.n_filters, V(obs.mjd.ctypes.data), V(obs.v.ctypes.data),
+            V(obs.w.ctypes.data), V(obs.filt.ctypes.data), V(obs.e_unit.ctypes.data), V(obs.s_unit.ctypes.data),
+            V(eph.ctypes.data), int(obs.t_min.size), V(obs.t_min.ctypes.data), V(obs.v_min.ctypes.data),
+            V(chi2.ctypes.data), V(dv.ctypes.data))
+        if rc:
+            raise RuntimeError(self.lib.refk_last_error().decode())
+        return chi2, dv

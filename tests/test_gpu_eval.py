@@ -1,10 +1,12 @@
 """chi^2 batch evaluation on the GPU (FP64 plain path) against the oracle.
 
 Tolerances: the oracle is compiled without fused multiply-adds and with the host libm, the
-kernel with nvcc's contractions and CUDA's libm, so results differ by rounding only.  For
-parameter vectors whose rotation the fixed-step RK4 resolves (h * L <= 0.5) the relative chi^2
-difference is bounded by RTOL_FP64; under-resolved vectors (RK4 unstable, chaotic in the last
-bit) are compared for agreement on finiteness only.  The 1e-12 bar is against the reference's
+kernel with nvcc's contractions and CUDA's libm, so the two differ by rounding only.  Rounding
+differences stay at that level for well-conditioned vectors and are amplified without bound where
+the fixed-step RK4 is unstable (fast or torque-spun-up rotation, Euler-angle poles).  Each
+vector's conditioning is measured on the oracle itself: chi^2 before and after moving every
+parameter by one ulp.  Vectors whose chi^2 moves by more than COND_LIMIT are ill-conditioned
+(a few percent) and are left out; all others must agree to RTOL_FP64.  The 1e-12 bar is against the reference's
 own kernel (tests/test_ref_kernel.py), which shares the compiler and libm.
 """
 import numpy as np
@@ -15,6 +17,25 @@ from asteroid_gb300 import api
 pytestmark = pytest.mark.gpu
 
 RTOL_FP64 = 1e-9
+COND_LIMIT = 1e-10
+
+
+def well_conditioned(oracle_mod, model, obs, P):
+    """Mask of vectors whose oracle chi^2 (in FP64, CHI_FLOAT = double) moves by at most
+    COND_LIMIT when every parameter is moved by one ulp, for three random sign patterns."""
+    acc_model = model
+    if not model.flags & api.ACC:
+        acc_model = api.make_model(model.flags | api.ACC, model.time_step, (2.0, 4800.0))
+        acc_model.ppsi1, acc_model.ppsi2 = model.ppsi1, model.ppsi2
+    a, _ = oracle_mod.chi2_batch(acc_model, obs, P)
+    rng = np.random.default_rng(0)
+    worst = np.zeros(len(P))
+    for _ in range(3):
+        Q = P * (1 + rng.choice([-1.0, 1.0], size=P.shape) * 2.3e-16)
+        b, _ = oracle_mod.chi2_batch(acc_model, obs, Q)
+        with np.errstate(invalid="ignore", divide="ignore"):
+            worst = np.maximum(worst, np.abs(a - b) / np.abs(a))
+    return np.isfinite(a) & np.isfinite(worst) & (worst <= COND_LIMIT)
 
 
 def _vectors(model, n, seed, reopt=0, resolved=True):
@@ -41,10 +62,11 @@ def test_fp64_matches_oracle(gpu, oracle_mod, synth_objects, name):
     with api.Engine(s.model, s.obs) as eng:
         chi2, dv = eng.eval(P)
     ref, ref_dv = oracle_mod.chi2_batch(s.model, s.obs, P)
-    both_nan = np.isnan(chi2) & np.isnan(ref)
-    ok = ~both_nan
-    assert np.all(np.isfinite(chi2[ok]) == np.isfinite(ref[ok]))
-    fin = ok & np.isfinite(ref)
+    good = well_conditioned(oracle_mod, s.model, s.obs, P)
+    assert good.sum() >= 0.5 * len(P), f"only {good.sum()} well-conditioned vectors"
+    assert good[-1], "the true model must be well conditioned"
+    assert np.all(np.isfinite(chi2[good]))
+    fin = good
     acc = bool(s.model.flags & api.ACC)
     rtol = RTOL_FP64 if acc else 2e-6  # without ACC chi2 is rounded to float (CHI_FLOAT)
     if s.model.flags & api.NUDGE:

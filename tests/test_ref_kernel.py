@@ -1,0 +1,76 @@
+"""The FP64 path against the reference's own kernel, at 1e-12 relative chi^2.
+
+oracle/_ref/ref_<variant>.cubin is the reference's cuda.c compiled for sm_100 from its sources
+(oracle/build_ref.sh, in the container that has the reference checkout); it travels with the
+tree to the GPU machine, where oracle/ref_gpu_loader.cpp runs its chi2one on the same inputs.
+Both sides run CUDA's libm with nvcc's multiply-add contractions, so the bar is the north-star
+1e-12 relative chi^2 (and delta_V), on every vector whose result is finite on both sides.
+"""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from asteroid_gb300 import api
+
+pytestmark = pytest.mark.gpu
+
+ROOT = Path(__file__).resolve().parents[1]
+GOLDEN = ROOT / "tests" / "golden"
+REF = ROOT / "oracle" / "_ref"
+FIXTURES = sorted(GOLDEN.glob("ref_*.json"))
+RTOL = 1e-12
+
+
+def _fixture(path):
+    from tests.test_oracle_pin import load_fixture
+
+    return load_fixture(path)
+
+
+def _compare(model, obs, P, variant, oracle_mod):
+    cubin = REF / f"ref_{variant}.cubin"
+    if not cubin.exists():
+        pytest.skip(f"{cubin.name} not built (needs the reference checkout where the tree was prepared)")
+    rk = oracle_mod.RefKernel(variant)
+    ref, ref_dv = rk.chi2_batch(model, obs, P)
+    with api.Engine(model, obs) as eng:
+        got, dv = eng.eval(P, api.PREC_FP64)
+    fin = np.isfinite(ref) & np.isfinite(got)
+    rel = np.abs(got[fin] - ref[fin]) / np.maximum(np.abs(ref[fin]), 1e-300)
+    nfin = np.isfinite(ref) != np.isfinite(got)
+    return rel, nfin, got, ref, dv, ref_dv
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=[p.stem for p in FIXTURES])
+def test_fp64_matches_reference_kernel_on_fixtures(gpu, oracle_mod, path):
+    fx, m, obs = _fixture(path)
+    rng = np.random.default_rng(17)
+    P = [np.array(p) for p in fx["params"]]
+    iL = api.param_names(m).index("L")
+    while len(P) < 64:
+        p = api.x2params(m, rng.uniform(0, 1, m.n_params), reopt=0)
+        if p is not None and p[iL] * m.time_step <= 0.5:
+            P.append(p)
+    rel, nfin, got, ref, dv, ref_dv = _compare(m, obs, np.array(P), fx["variant"], oracle_mod)
+    assert not nfin.any()
+    assert rel.size > 0 and rel.max() <= RTOL, f"max rel {rel.max():.3e}"
+    fin = np.isfinite(ref)
+    assert np.allclose(dv[fin], ref_dv[fin], rtol=RTOL, atol=1e-13)
+
+
+@pytest.mark.parametrize("name,variant", [("c0acc", "ppsi_torque_acc"), ("c2", "c2_nudge_acc")])
+def test_fp64_matches_reference_kernel_on_configs(gpu, oracle_mod, synth_objects, name, variant):
+    s = synth_objects(name)
+    m = s.model
+    rng = np.random.default_rng(23)
+    iL = api.param_names(m).index("L")
+    P = [s.params_true]
+    while len(P) < 96:
+        p = api.x2params(m, rng.uniform(0, 1, m.n_params), reopt=0)
+        if p is not None and p[iL] * m.time_step <= 0.5:
+            P.append(p)
+    rel, nfin, *_ = _compare(m, s.obs, np.array(P), variant, oracle_mod)
+    assert not nfin.any()
+    assert rel.max() <= RTOL, f"max rel {rel.max():.3e}"
