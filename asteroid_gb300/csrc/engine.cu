@@ -117,6 +117,11 @@ __global__ void __launch_bounds__(128) eval_kernel(DevModel M, const void* g_obs
 {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t bar;
+    __shared__ float4 trig[PREC == AST_PREC_MIXED ? kTrigTable : 1];
+    if (PREC == AST_PREC_MIXED) {
+        trig_table_fill(trig);
+        __syncthreads();
+    }
     const bool staged = use_smem ? bulk_stage(smem, g_obs, (uint32_t)L.bytes, &bar, err) : false;
     const ObsView o = L.view(staged ? (const void*)smem : g_obs, M.n_data);
     const int N = M.n_params;
@@ -129,7 +134,7 @@ __global__ void __launch_bounds__(128) eval_kernel(DevModel M, const void* g_obs
         if (PREC == AST_PREC_FP64)
             r = chi2_fp64<CF>(M, o, p, d);
         else
-            r = chi2_mixed<CF>(M, o, p, d);
+            r = chi2_mixed<CF>(M, o, p, d, trig);
         chi2[k] = (double)r;
         if (dv)
             for (int m = 0; m < M.n_filters; m++) dv[k * M.n_filters + m] = (double)d[m];

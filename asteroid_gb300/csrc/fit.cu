@@ -153,10 +153,11 @@ __device__ void start_chain(const DevModel& M, const FitView<CF>& V, int64_t s, 
 }
 
 template <class CF, int PREC>
-__device__ __forceinline__ CF eval_point(const DevModel& M, const ObsView& o, const double* params, CF* dv)
+__device__ __forceinline__ CF eval_point(const DevModel& M, const ObsView& o, const double* params, CF* dv,
+                                         const float4* trig)
 {
     if (PREC == AST_PREC_FP64) return chi2_fp64<CF>(M, o, params, dv);
-    return chi2_mixed<CF>(M, o, params, dv);
+    return chi2_mixed<CF>(M, o, params, dv, trig);
 }
 
 template <class CF, int PREC>
@@ -165,6 +166,11 @@ __global__ void __launch_bounds__(256) fit_kernel(DevModel M, const void* g_obs,
 {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t bar;
+    __shared__ float4 trig[PREC == AST_PREC_MIXED ? kTrigTable : 1];
+    if (PREC == AST_PREC_MIXED) {
+        trig_table_fill(trig);
+        __syncthreads();
+    }
     const bool staged = use_smem ? bulk_stage(smem, g_obs, (uint32_t)L.bytes, &bar, &V.ctr[4]) : false;
     const ObsView o = L.view(staged ? (const void*)smem : g_obs, M.n_data);
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -212,7 +218,7 @@ __global__ void __launch_bounds__(256) fit_kernel(DevModel M, const void* g_obs,
             const int rej = x2params<CF>(M, V.reopt, p, params);
             CF fv = HUGEV;
             if (!rej) {
-                fv = eval_point<CF, PREC>(M, o, params, dvl);
+                fv = eval_point<CF, PREC>(M, o, params, dvl, trig);
                 ev++;
                 n_ev++;
             }

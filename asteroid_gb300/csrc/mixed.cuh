@@ -1,74 +1,74 @@
-// mixed.cuh -- the mixed-precision chi^2: FP32 right-hand side and brightness, FP64 state.
+// mixed.cuh -- the mixed-precision chi^2.
 //
-// GB300 runs FP32 FMAs at 64x the FP64 rate, so the plain path is bound by the FP64 pipe.
-// Here the Euler-equation / Euler-angle right-hand side (cuda.c:44-75) and the brightness
-// model (cuda.c:432-689) are evaluated in FP32 from angles first reduced to [-pi, pi) in
-// FP64, while the RK4 state and its stage updates stay in FP64 (rotation phase grows to
-// ~1e5 rad over a long light curve, where one FP32 ulp is ~0.008 rad), and the per-filter
-// sums and the chi^2 are accumulated in FP64.  Error against the FP64 path is measured by
-// tests/test_mixed.py and reported by bench.py.
+// GB300 executes FP32 FMAs at 64x its FP64 rate, so the plain path (cuda.c's arithmetic, all
+// FP64) is bound by the FP64 pipe.  Here the fixed-step RK4 of the Euler equations and Euler
+// angles (cuda.c:13-77, 319-372) runs entirely on the FP32 pipe: the state, the stage
+// combinations and the right-hand side (including sin/cos of the Euler angles) are double-float
+// values (dfloat.cuh), ~48-bit significands, which keeps the integrated rotation phase (up to
+// ~1e5 rad over a long light curve) accurate to ~1e-10 rad.  The brightness model at each
+// observation (cuda.c:432-689) is evaluated in plain FP32 from the double-float angles reduced
+// to [-pi, pi].  FP64 is left for the per-evaluation set-up (initial angles and angular
+// velocity, cuda.c:195-252), the parameter-independent ephemeris interpolation (hoisted per
+// object) and the per-filter sums and chi^2 (cuda.c:707-714, 887-910).
 #pragma once
 #include <math.h>
+#include "dfloat.cuh"
 #include "model.cuh"
 
 namespace ast {
 
-// x reduced to [-pi, pi) in FP64 with a two-term 2*pi (Cody-Waite), then rounded to FP32.
-__device__ __forceinline__ float reduce_angle_f(double x)
+struct DfOde {
+    df mu[6];
+};
+
+__device__ __forceinline__ void ode_torque_df(const df* y, df* f, const df* mu, const float4* tab)
 {
-    const double k = rint(x * 0.15915494309189535);       // 1 / (2 pi)
-    const double r = fma(-k, 6.283185307179586, x);        // 2 pi, high part
-    return (float)fma(-k, 2.4492935982947064e-16, r);      // 2 pi, low part
+    df s5, c5, s4, c4;
+    df_sincos(y[5], tab, &s5, &c5);
+    df_sincos(y[4], tab, &s4, &c4);
+    f[0] = df_add(df_mul(df_mul(mu[0], y[1]), y[2]), mu[3]);
+    f[1] = df_add(df_mul(df_mul(mu[1], y[2]), y[0]), mu[4]);
+    f[2] = df_add(df_mul(df_mul(mu[2], y[0]), y[1]), mu[5]);
+    f[3] = df_div(df_add(df_mul(y[0], s5), df_mul(y[1], c5)), s4);
+    f[4] = df_sub(df_mul(y[0], c5), df_mul(y[1], s5));
+    f[5] = df_sub(y[2], df_mul(f[3], c4));
 }
 
-__device__ __forceinline__ void ode_torque_f(const double* y, float* f, const float* mu)
+__device__ __forceinline__ void ode_free_df(const df* y, df* f, const df* mu, const float4* tab)
 {
-    float s5, c5, s4, c4;
-    sincosf(reduce_angle_f(y[5]), &s5, &c5);
-    sincosf(reduce_angle_f(y[4]), &s4, &c4);
-    const float y0 = (float)y[0], y1 = (float)y[1], y2 = (float)y[2];
-    f[0] = mu[0] * y1 * y2 + mu[3];
-    f[1] = mu[1] * y2 * y0 + mu[4];
-    f[2] = mu[2] * y0 * y1 + mu[5];
-    f[3] = (y0 * s5 + y1 * c5) / s4;
-    f[4] = y0 * c5 - y1 * s5;
-    f[5] = y2 - f[3] * c4;
-}
-
-__device__ __forceinline__ void ode_free_f(const double* y, float* f, const float* mu)
-{
-    float s2, c2, s1, c1;
-    sincosf(reduce_angle_f(2.0 * y[2]), &s2, &c2);
-    sincosf(reduce_angle_f(y[1]), &s1, &c1);
-    f[0] = mu[0] * (mu[1] - mu[2] * c2);
-    f[1] = mu[0] * mu[2] * s1 * s2;
-    f[2] = c1 * (mu[0] - f[0]);
+    df s2, c2, s1, c1;
+    df_sincos(df{2.0f * y[2].hi, 2.0f * y[2].lo}, tab, &s2, &c2);
+    df_sincos(y[1], tab, &s1, &c1);
+    f[0] = df_mul(mu[0], df_sub(mu[1], df_mul(mu[2], c2)));
+    f[1] = df_mul(df_mul(df_mul(mu[0], mu[2]), s1), s2);
+    f[2] = df_mul(c1, df_sub(mu[0], f[0]));
 }
 
 template <int NODE>
-__device__ __forceinline__ void rk4_step_mixed(double* y, double h, const float* mu)
+__device__ __forceinline__ void rk4_step_df(df* y, df hh, df h, df h6, const df* mu, const float4* tab)
 {
-    double f[NODE];
-    float K1[NODE], K2[NODE], K3[NODE], K4[NODE];
-    const double hh = 0.5 * h;
-    if (NODE == 6) ode_torque_f(y, K1, mu); else ode_free_f(y, K1, mu);
+    df f[NODE], K1[NODE], K2[NODE], K3[NODE], K4[NODE];
+    if (NODE == 6) ode_torque_df(y, K1, mu, tab); else ode_free_df(y, K1, mu, tab);
 #pragma unroll
-    for (int j = 0; j < NODE; j++) f[j] = fma(hh, (double)K1[j], y[j]);
-    if (NODE == 6) ode_torque_f(f, K2, mu); else ode_free_f(f, K2, mu);
+    for (int j = 0; j < NODE; j++) f[j] = df_add(y[j], df_mul(hh, K1[j]));
+    if (NODE == 6) ode_torque_df(f, K2, mu, tab); else ode_free_df(f, K2, mu, tab);
 #pragma unroll
-    for (int j = 0; j < NODE; j++) f[j] = fma(hh, (double)K2[j], y[j]);
-    if (NODE == 6) ode_torque_f(f, K3, mu); else ode_free_f(f, K3, mu);
+    for (int j = 0; j < NODE; j++) f[j] = df_add(y[j], df_mul(hh, K2[j]));
+    if (NODE == 6) ode_torque_df(f, K3, mu, tab); else ode_free_df(f, K3, mu, tab);
 #pragma unroll
-    for (int j = 0; j < NODE; j++) f[j] = fma(h, (double)K3[j], y[j]);
-    if (NODE == 6) ode_torque_f(f, K4, mu); else ode_free_f(f, K4, mu);
-    const double h6 = h * (1 / 6.0);
+    for (int j = 0; j < NODE; j++) f[j] = df_add(y[j], df_mul(h, K3[j]));
+    if (NODE == 6) ode_torque_df(f, K4, mu, tab); else ode_free_df(f, K4, mu, tab);
 #pragma unroll
-    for (int j = 0; j < NODE; j++) y[j] = fma(h6, (double)(K1[j] + 2.0f * (K2[j] + K3[j]) + K4[j]), y[j]);
+    for (int j = 0; j < NODE; j++) {
+        const df s23 = df_add(K2[j], K3[j]);
+        const df s = df_add(df_add(K1[j], K4[j]), df{2.0f * s23.hi, 2.0f * s23.lo});
+        y[j] = df_add(y[j], df_mul(h6, s));
+    }
 }
 
-// Same contract as chi2_fp64 (model.cuh).
+// Same contract as chi2_fp64 (model.cuh); tab is the shared-memory sin/cos table.
 template <class CF>
-__device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const double* params, CF* delta_V)
+__device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const double* params, CF* delta_V, const float4* tab)
 {
     const int flags = M.flags;
     const ast_type_ids& T = M.t;
@@ -80,7 +80,7 @@ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const double* para
     float t_old[2] = {0.f, 0.f}, V_old[2] = {0.f, 0.f};
 
 #define AST_P(tt) params[M.idx[T.tt]]
-    // Parameter-level set-up in FP64 (once per evaluation).
+    // Per-evaluation set-up in FP64.
     const double th_M = AST_P(theta_M), ph_M = AST_P(phi_M);
     const double M_xd = sin(th_M) * cos(ph_M), M_yd = sin(th_M) * sin(ph_M), M_zd = cos(th_M);
     const double XMd = sqrt(M_zd * M_zd + M_xd * M_xd);
@@ -92,36 +92,36 @@ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const double* para
     const double Ii = (1.0 + ct * ct) / (bt * bt + ct * ct);
     const double Is_inv = 1.0 / Is, Ii_inv = 1.0 / Ii;
     const double psi0 = AST_P(psi_0);
-    double y[6];
-    float mu[6];
+    df y[6];
+    df mu[6];
     const bool torque = (flags & AST_TORQUE) != 0;
     {
         const double theta = asin(sqrt((AST_P(Es) - 1.0) / (sin(psi0) * sin(psi0) * (Ii_inv - Is_inv) + Is_inv - 1.0)));
         if (torque) {
-            mu[0] = (float)((Is - 1.0) * Ii_inv);
-            mu[1] = (float)((1.0 - Ii) * Is_inv);
-            mu[2] = (float)(Ii - Is);
-            mu[3] = (float)AST_P(Ti);
-            mu[4] = (float)AST_P(Ts);
-            mu[5] = (float)AST_P(Tl);
+            mu[0] = df_from_double((Is - 1.0) * Ii_inv);
+            mu[1] = df_from_double((1.0 - Ii) * Is_inv);
+            mu[2] = df_from_double(Ii - Is);
+            mu[3] = df_from_double(AST_P(Ti));
+            mu[4] = df_from_double(AST_P(Ts));
+            mu[5] = df_from_double(AST_P(Tl));
             const double L = AST_P(L);
-            y[0] = L * Ii_inv * sin(theta) * sin(psi0);
-            y[1] = L * Is_inv * sin(theta) * cos(psi0);
-            y[2] = L * cos(theta);
-            y[3] = AST_P(phi_0);
-            y[4] = theta;
-            y[5] = psi0;
+            y[0] = df_from_double(L * Ii_inv * sin(theta) * sin(psi0));
+            y[1] = df_from_double(L * Is_inv * sin(theta) * cos(psi0));
+            y[2] = df_from_double(L * cos(theta));
+            y[3] = df_from_double(AST_P(phi_0));
+            y[4] = df_from_double(theta);
+            y[5] = df_from_double(psi0);
         } else {
-            mu[0] = (float)AST_P(L);
-            mu[1] = (float)(0.5 * (Ii_inv + Is_inv));
-            mu[2] = (float)(0.5 * (Ii_inv - Is_inv));
-            y[0] = AST_P(phi_0);
-            y[1] = theta;
-            y[2] = psi0;
+            mu[0] = df_from_double(AST_P(L));
+            mu[1] = df_from_double(0.5 * (Ii_inv + Is_inv));
+            mu[2] = df_from_double(0.5 * (Ii_inv - Is_inv));
+            y[0] = df_from_double(AST_P(phi_0));
+            y[1] = df_from_double(theta);
+            y[2] = df_from_double(psi0);
         }
     }
     const bool bw = (flags & AST_BW_BALL) != 0;
-    float b_ph = 0, c_ph = 0, kappa = 0, cos_phR = 0, sin_phR = 0, cos_thR = 0, sin_thR = 0;
+    float b_ph = 1, c_ph = 1, kappa = 0, cos_phR = 0, sin_phR = 0, cos_thR = 0, sin_thR = 0;
     if (bw) {
         kappa = (float)AST_P(kappa);
         sincosf((float)AST_P(phi_R), &sin_phR, &cos_phR);
@@ -135,16 +135,17 @@ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const double* para
     for (int i = 0; i < N_data; i++) {
         if (i > 0) {
             const int N_steps = o.nst[i];
-            const double h = o.h[i];
+            const double hd = o.h[i];
+            const df h = df_from_double(hd), hh = df_from_double(0.5 * hd), h6 = df_from_double(hd / 6.0);
             if (torque)
-                for (int l = 0; l < N_steps; l++) rk4_step_mixed<6>(y, h, mu);
+                for (int l = 0; l < N_steps; l++) rk4_step_df<6>(y, hh, h, h6, mu, tab);
             else
-                for (int l = 0; l < N_steps; l++) rk4_step_mixed<3>(y, h, mu);
+                for (int l = 0; l < N_steps; l++) rk4_step_df<3>(y, hh, h, h6, mu, tab);
         }
         float sin_phi, cos_phi, sin_theta, cos_theta, sin_psi, cos_psi;
-        sincosf(reduce_angle_f(torque ? y[3] : y[0]), &sin_phi, &cos_phi);
-        sincosf(reduce_angle_f(torque ? y[4] : y[1]), &sin_theta, &cos_theta);
-        sincosf(reduce_angle_f(torque ? y[5] : y[2]), &sin_psi, &cos_psi);
+        sincosf(df_reduce_f(torque ? y[3] : y[0]), &sin_phi, &cos_phi);
+        sincosf(df_reduce_f(torque ? y[4] : y[1]), &sin_theta, &cos_theta);
+        sincosf(df_reduce_f(torque ? y[5] : y[2]), &sin_psi, &cos_psi);
         float N_x = XM_x * cos_phi + YM_x * sin_phi;
         float N_y = YM_y * sin_phi;
         float N_z = XM_z * cos_phi + YM_z * sin_phi;
