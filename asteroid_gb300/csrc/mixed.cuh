@@ -17,11 +17,117 @@
 
 namespace ast {
 
+// f(t) = t - (1 - t^2) atanh(t) for 0 <= t < 1, without cancellation: for t < 1/2 the series
+// sum_k 2 t^(2k+1) / ((2k-1)(2k+1)), else the closed form (cancellation at most 6x there).
+AST_HD float ls_f(float t)
+{
+    const float t2 = t * t;
+    if (t < 0.5f) {
+        float p = 2.0f / 575.0f;  // k = 12
+        p = fmaf(p, t2, 2.0f / 483.0f);
+        p = fmaf(p, t2, 2.0f / 399.0f);
+        p = fmaf(p, t2, 2.0f / 323.0f);
+        p = fmaf(p, t2, 2.0f / 255.0f);
+        p = fmaf(p, t2, 2.0f / 195.0f);
+        p = fmaf(p, t2, 2.0f / 143.0f);
+        p = fmaf(p, t2, 2.0f / 99.0f);
+        p = fmaf(p, t2, 2.0f / 63.0f);
+        p = fmaf(p, t2, 2.0f / 35.0f);
+        p = fmaf(p, t2, 2.0f / 15.0f);
+        p = fmaf(p, t2, 2.0f / 3.0f);
+        return p * t2 * t;
+    }
+    return t - (1.0f - t2) * 0.5f * log1pf(2.0f * t / (1.0f - t));
+}
+
+// Lommel-Seeliger ellipsoid magnitude, Muinonen & Lumme (2015) eqs. 10-14 as in cuda.c:664-689,
+// rearranged for FP32.  Sp, Ep: unit Sun and Earth vectors in the body frame (b, c, a);
+// ib = 1/b, ic = 1/c; bc = b*c.  Exact identities replace the two cancellations of the
+// reference's form, which amplify FP32 rounding by up to ~(1/c)^2 for flattened bodies:
+//  * scalar = |S' + E'| of the scaled vectors S' = (Sb/b, Sc/c, Sa), E' likewise, computed from
+//    the body-frame half vector S + E instead of sqrt(sS^2 + sE^2 + 2 sS sE cos alpha');
+//  * with mu = lambda', nu = alpha' - lambda' (each from atan2 of a cross and a dot product),
+//    cos(lambda'-alpha') + cos lambda' + sin lambda' sin(lambda'-alpha') ln(cot(mu/2) cot(nu/2))
+//    = 2 D^2 f(s/D), D = cos((mu - nu)/2), s = cos((mu + nu)/2), f as in ls_f.
+AST_HD float ls_magnitude_f(float Sb, float Sc, float Sa, float Eb, float Ec, float Ea, float ib, float ic, float bc)
+{
+    const float sx = Sb * ib, sy = Sc * ic, sz = Sa;
+    const float ex = Eb * ib, ey = Ec * ic, ez = Ea;
+    const float hx = (Sb + Eb) * ib, hy = (Sc + Ec) * ic, hz = Sa + Ea;
+    const float sS = sqrtf(sx * sx + sy * sy + sz * sz);
+    const float sE = sqrtf(ex * ex + ey * ey + ez * ez);
+    const float scalar = sqrtf(hx * hx + hy * hy + hz * hz);
+    const float cx = sy * ez - sz * ey, cy = sz * ex - sx * ez, cz = sx * ey - sy * ex;
+    const float cn = sqrtf(cx * cx + cy * cy + cz * cz);  // |S' x E'| = |S' x H'| = |H' x E'|
+    const float mu = atan2f(cn, sx * hx + sy * hy + sz * hz);
+    const float nu = atan2f(cn, hx * ex + hy * ey + hz * ez);
+    const float D = cosf(0.5f * (mu - nu));
+    // s = cos(alpha'/2) = sin(eps/2) with eps = pi - alpha' taken directly from the vectors.
+    const float s = sinf(0.5f * atan2f(cn, -(sx * ex + sy * ey + sz * ez)));
+    const float B = 2.0f * D * D * ls_f(s / D);
+    return -2.5f * log10f(bc * sS * sE / scalar * B);
+}
+
+// FP64 model magnitude at observation i for Euler angles ang = (phi, theta, psi), with the
+// reference's expressions (cuda.c:195-217, 432-689).  Used by the mixed path only where the
+// NUDGE minimum detection needs magnitudes exact to FP64 rounding.
+AST_HD double vmod_fp64(const DevModel& M, const ObsView& o, const double* params, const double* ang, int i)
+{
+    const ast_type_ids& T = M.t;
+#define AST_Q(tt) params[M.idx[T.tt]]
+    const double th_M = AST_Q(theta_M), ph_M = AST_Q(phi_M);
+    const double M_x = sin(th_M) * cos(ph_M), M_y = sin(th_M) * sin(ph_M), M_z = cos(th_M);
+    const double XM = sqrt(M_z * M_z + M_x * M_x);
+    const double XM_x = M_z / XM, XM_z = -M_x / XM;
+    const double YM_x = M_y * XM_z, YM_y = M_z * XM_x - M_x * XM_z, YM_z = -M_y * XM_x;
+    const double cos_phi = cos(ang[0]), sin_phi = sin(ang[0]);
+    const double N_x = XM_x * cos_phi + YM_x * sin_phi, N_y = YM_y * sin_phi, N_z = XM_z * cos_phi + YM_z * sin_phi;
+    const double p_x = N_y * M_z - N_z * M_y, p_y = N_z * M_x - N_x * M_z, p_z = N_x * M_y - N_y * M_x;
+    const double cos_theta = cos(ang[1]), sin_theta = sin(ang[1]);
+    double a_x = M_x * cos_theta + p_x * sin_theta, a_y = M_y * cos_theta + p_y * sin_theta,
+           a_z = M_z * cos_theta + p_z * sin_theta;
+    const double w_x = a_y * N_z - a_z * N_y, w_y = a_z * N_x - a_x * N_z, w_z = a_x * N_y - a_y * N_x;
+    const double sin_psi = sin(ang[2]), cos_psi = cos(ang[2]);
+    const double b_x = N_x * cos_psi + w_x * sin_psi, b_y = N_y * cos_psi + w_y * sin_psi,
+                 b_z = N_z * cos_psi + w_z * sin_psi;
+    const double c_x = a_y * b_z - a_z * b_y, c_y = a_z * b_x - a_x * b_z, c_z = a_x * b_y - a_y * b_x;
+    const double E_x1 = o.ex[i], E_y1 = o.ey[i], E_z1 = o.ez[i], S_x1 = o.sx[i], S_y1 = o.sy[i], S_z1 = o.sz[i];
+    if (M.flags & AST_BW_BALL) {
+        const double cR = cos(AST_Q(phi_R)), sR = sin(AST_Q(phi_R)), cT = cos(AST_Q(theta_R)), sT = sin(AST_Q(theta_R));
+        const double Nx = b_x * cR + c_x * sR, Ny = b_y * cR + c_y * sR, Nz = b_z * cR + c_z * sR;
+        const double px = Ny * a_z - Nz * a_y, py = Nz * a_x - Nx * a_z, pz = Nx * a_y - Ny * a_x;
+        a_x = a_x * cT + px * sT;
+        a_y = a_y * cT + py * sT;
+        a_z = a_z * cT + pz * sT;
+        const double cos_zeta = a_x * E_x1 + a_y * E_y1 + a_z * E_z1;
+        return -2.5 * log10(0.5 * (AST_Q(kappa) * (1 + cos_zeta) + 0.5 * (1 - cos_zeta)));
+    }
+    const double Ep_b = b_x * E_x1 + b_y * E_y1 + b_z * E_z1, Ep_c = c_x * E_x1 + c_y * E_y1 + c_z * E_z1,
+                 Ep_a = a_x * E_x1 + a_y * E_y1 + a_z * E_z1;
+    const double Sp_b = b_x * S_x1 + b_y * S_y1 + b_z * S_z1, Sp_c = c_x * S_x1 + c_y * S_y1 + c_z * S_z1,
+                 Sp_a = a_x * S_x1 + a_y * S_y1 + a_z * S_z1;
+    const double b = (M.flags & AST_BC) ? AST_Q(b) : AST_Q(b_tumb);
+    const double c = (M.flags & AST_BC) ? AST_Q(c) : AST_Q(c_tumb);
+#undef AST_Q
+    const double scalar_Sun = sqrt(Sp_b * Sp_b / (b * b) + Sp_c * Sp_c / (c * c) + Sp_a * Sp_a);
+    const double scalar_Earth = sqrt(Ep_b * Ep_b / (b * b) + Ep_c * Ep_c / (c * c) + Ep_a * Ep_a);
+    const double cos_alpha_p = (Sp_b * Ep_b / (b * b) + Sp_c * Ep_c / (c * c) + Sp_a * Ep_a) / (scalar_Sun * scalar_Earth);
+    const double sin_alpha_p = sqrt(1.0 - cos_alpha_p * cos_alpha_p);
+    const double alpha_p = atan2(sin_alpha_p, cos_alpha_p);
+    const double scalar = sqrt(scalar_Sun * scalar_Sun + scalar_Earth * scalar_Earth + 2 * scalar_Sun * scalar_Earth * cos_alpha_p);
+    const double cos_lambda_p = (scalar_Sun + scalar_Earth * cos_alpha_p) / scalar;
+    const double sin_lambda_p = scalar_Earth * sin_alpha_p / scalar;
+    const double lambda_p = atan2(sin_lambda_p, cos_lambda_p);
+    return -2.5 * log10(b * c * scalar_Sun * scalar_Earth / scalar *
+                        (cos(lambda_p - alpha_p) + cos_lambda_p +
+                         sin_lambda_p * sin(lambda_p - alpha_p) * log(1.0 / tan(0.5 * lambda_p) / tan(0.5 * (alpha_p - lambda_p)))));
+}
+
 struct DfOde {
     df mu[6];
 };
 
-__device__ __forceinline__ void ode_torque_df(const df* y, df* f, const df* mu, const float4* tab)
+AST_HD void ode_torque_df(const df* y, df* f, const df* mu, const float4* tab)
 {
     df s5, c5, s4, c4;
     df_sincos(y[5], tab, &s5, &c5);
@@ -34,7 +140,7 @@ __device__ __forceinline__ void ode_torque_df(const df* y, df* f, const df* mu, 
     f[5] = df_sub(y[2], df_mul(f[3], c4));
 }
 
-__device__ __forceinline__ void ode_free_df(const df* y, df* f, const df* mu, const float4* tab)
+AST_HD void ode_free_df(const df* y, df* f, const df* mu, const float4* tab)
 {
     df s2, c2, s1, c1;
     df_sincos(df{2.0f * y[2].hi, 2.0f * y[2].lo}, tab, &s2, &c2);
@@ -45,7 +151,7 @@ __device__ __forceinline__ void ode_free_df(const df* y, df* f, const df* mu, co
 }
 
 template <int NODE>
-__device__ __forceinline__ void rk4_step_df(df* y, df hh, df h, df h6, const df* mu, const float4* tab)
+AST_HD void rk4_step_df(df* y, df hh, df h, df h6, const df* mu, const float4* tab)
 {
     df f[NODE], K1[NODE], K2[NODE], K3[NODE], K4[NODE];
     if (NODE == 6) ode_torque_df(y, K1, mu, tab); else ode_free_df(y, K1, mu, tab);
@@ -68,7 +174,7 @@ __device__ __forceinline__ void rk4_step_df(df* y, df hh, df h, df h6, const df*
 
 // Same contract as chi2_fp64 (model.cuh); tab is the shared-memory sin/cos table.
 template <class CF>
-__device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const double* params, CF* delta_V, const float4* tab)
+__host__ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const double* params, CF* delta_V, const float4* tab)
 {
     const int flags = M.flags;
     const ast_type_ids& T = M.t;
@@ -78,6 +184,7 @@ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const double* para
     int Mmin = 0;
     float t_mod[AST_M_MAX], V_mod[AST_M_MAX];
     float t_old[2] = {0.f, 0.f}, V_old[2] = {0.f, 0.f};
+    double ang_old[2][3] = {{0, 0, 0}, {0, 0, 0}};
 
 #define AST_P(tt) params[M.idx[T.tt]]
     // Per-evaluation set-up in FP64.
@@ -130,7 +237,7 @@ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const double* para
         b_ph = (float)((flags & AST_BC) ? AST_P(b) : bt);
         c_ph = (float)((flags & AST_BC) ? AST_P(c) : ct);
     }
-    const float ib2 = 1.0f / (b_ph * b_ph), ic2 = 1.0f / (c_ph * c_ph);
+    const float ib = 1.0f / b_ph, ic = 1.0f / c_ph;
 
     for (int i = 0; i < N_data; i++) {
         if (i > 0) {
@@ -186,20 +293,7 @@ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const double* para
             const float Sp_b = b_x * S_x1 + b_y * S_y1 + b_z * S_z1;
             const float Sp_c = c_x * S_x1 + c_y * S_y1 + c_z * S_z1;
             const float Sp_a = a_x * S_x1 + a_y * S_y1 + a_z * S_z1;
-            const float sS = sqrtf(Sp_b * Sp_b * ib2 + Sp_c * Sp_c * ic2 + Sp_a * Sp_a);
-            const float sE = sqrtf(Ep_b * Ep_b * ib2 + Ep_c * Ep_c * ic2 + Ep_a * Ep_a);
-            const float cos_alpha_p = (Sp_b * Ep_b * ib2 + Sp_c * Ep_c * ic2 + Sp_a * Ep_a) / (sS * sE);
-            const float sin_alpha_p = sqrtf(fmaxf(0.0f, 1.0f - cos_alpha_p * cos_alpha_p));
-            const float alpha_p = atan2f(sin_alpha_p, cos_alpha_p);
-            const float scalar = sqrtf(sS * sS + sE * sE + 2 * sS * sE * cos_alpha_p);
-            const float cos_lambda_p = (sS + sE * cos_alpha_p) / scalar;
-            const float sin_lambda_p = sE * sin_alpha_p / scalar;
-            const float lambda_p = atan2f(sin_lambda_p, cos_lambda_p);
-            float s_la, c_la;
-            sincosf(lambda_p - alpha_p, &s_la, &c_la);
-            Vmod = -2.5f * log10f(b_ph * c_ph * sS * sE / scalar *
-                                  (c_la + cos_lambda_p +
-                                   sin_lambda_p * s_la * logf(1.0f / tanf(0.5f * lambda_p) / tanf(0.5f * (alpha_p - lambda_p)))));
+            Vmod = ls_magnitude_f(Sp_b, Sp_c, Sp_a, Ep_b, Ep_c, Ep_a, ib, ic, b_ph * c_ph);
         }
         {
             const int m = o.f[i];
@@ -210,30 +304,43 @@ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const double* para
             sum_w[m] = sum_w[m] + wi;
         }
         if (flags & AST_NUDGE) {
-            if (i < 2) {
-                t_old[i] = (float)o.t[i];
-                V_old[i] = Vmod;
-            } else {
-                if (V_old[1] > V_old[0] && V_old[1] >= Vmod) {
-                    bool local = false;
-                    for (int ii = 0; ii < M.n_min; ii++)
-                        if (fabsf(t_old[1] - M.t_min[ii]) < AST_DT_MAX2) local = true;
-                    if (local) {
+            // Model minima near observed minima (cuda.c:716-760).  The detection and the parabola
+            // are discontinuous in the magnitudes (the reference even rounds them to float), so an
+            // FP32 magnitude is used only to rule a triple out with a margin far above its error;
+            // a candidate triple is re-evaluated in FP64 from the double-float angles and tested
+            // exactly as the reference tests it.
+            const double ang_i[3] = {df_to_double(torque ? y[3] : y[0]), df_to_double(torque ? y[4] : y[1]),
+                                     df_to_double(torque ? y[5] : y[2])};
+            if (i >= 2) {
+                bool local = false;
+                for (int ii = 0; ii < M.n_min; ii++)
+                    if (fabsf(t_old[1] - M.t_min[ii]) < AST_DT_MAX2) local = true;
+                const float margin = 1e-4f;
+                if (local && V_old[1] > V_old[0] - margin && V_old[1] >= Vmod - margin) {
+                    const float f0 = (float)vmod_fp64(M, o, params, ang_old[0], i - 2);
+                    const float f1 = (float)vmod_fp64(M, o, params, ang_old[1], i - 1);
+                    const double v2 = vmod_fp64(M, o, params, ang_i, i);
+                    if (f1 > f0 && f1 >= v2) {
                         Mmin++;
                         if (Mmin > AST_M_MAX) return (CF)kHuge;
                         const double ti = o.t[i];
-                        const double a = (((double)Vmod - V_old[1]) / (ti - t_old[1]) - (V_old[1] - V_old[0]) / (t_old[1] - t_old[0])) / (ti - t_old[0]);
-                        const double b = (V_old[1] - V_old[0]) / (t_old[1] - t_old[0]) - a * (t_old[1] + t_old[0]);
-                        const double c = V_old[1] - a * t_old[1] * t_old[1] - b * t_old[1];
+                        const double a = ((v2 - f1) / (ti - t_old[1]) - (f1 - f0) / (t_old[1] - t_old[0])) / (ti - t_old[0]);
+                        const double b = (f1 - f0) / (t_old[1] - t_old[0]) - a * (t_old[1] + t_old[0]);
+                        const double c = f1 - a * t_old[1] * t_old[1] - b * t_old[1];
                         t_mod[Mmin - 1] = (float)(-b / 2.0 / a);
                         V_mod[Mmin - 1] = (float)(a * t_mod[Mmin - 1] * t_mod[Mmin - 1] + b * t_mod[Mmin - 1] + c);
                     }
                 }
+            }
+            const int slot = i < 2 ? i : 1;
+            if (i >= 2) {
                 t_old[0] = t_old[1];
                 V_old[0] = V_old[1];
-                t_old[1] = (float)o.t[i];
-                V_old[1] = Vmod;
+                for (int k = 0; k < 3; k++) ang_old[0][k] = ang_old[1][k];
             }
+            t_old[slot] = (float)o.t[i];
+            V_old[slot] = Vmod;
+            for (int k = 0; k < 3; k++) ang_old[slot][k] = ang_i[k];
         }
     }
 #undef AST_P

@@ -272,21 +272,26 @@ AST_HD void params2x(const DevModel& M, const double* params, CF* x)
 // Ki/Ii, Ks/Is, Kl/Il) with Il = 1.
 __device__ __forceinline__ void ode_torque(const double* y, double* f, const double* mu)
 {
-    // Separate sin/cos calls as in the reference, so the compiler treats them identically.
+    double s5, c5, s4, c4;
+    sincos(y[5], &s5, &c5);
+    sincos(y[4], &s4, &c4);
     f[0] = mu[0] * y[1] * y[2] + mu[3];
     f[1] = mu[1] * y[2] * y[0] + mu[4];
     f[2] = mu[2] * y[0] * y[1] + mu[5];
-    f[3] = (y[0] * sin(y[5]) + y[1] * cos(y[5])) / sin(y[4]);
-    f[4] = y[0] * cos(y[5]) - y[1] * sin(y[5]);
-    f[5] = y[2] - f[3] * cos(y[4]);
+    f[3] = (y[0] * s5 + y[1] * c5) / s4;
+    f[4] = y[0] * c5 - y[1] * s5;
+    f[5] = y[2] - f[3] * c4;
 }
 
 // Torque-free Euler angles (cuda.c:68-75): y = (phi, theta, psi), mu = (L, Ip, Im).
 __device__ __forceinline__ void ode_free(const double* y, double* f, const double* mu)
 {
-    f[0] = mu[0] * (mu[1] - mu[2] * cos(2.0 * y[2]));
-    f[1] = mu[0] * mu[2] * sin(y[1]) * sin(2.0 * y[2]);
-    f[2] = cos(y[1]) * (mu[0] - f[0]);
+    double s2, c2, s1, c1;
+    sincos(2.0 * y[2], &s2, &c2);
+    sincos(y[1], &s1, &c1);
+    f[0] = mu[0] * (mu[1] - mu[2] * c2);
+    f[1] = mu[0] * mu[2] * s1 * s2;
+    f[2] = c1 * (mu[0] - f[0]);
 }
 
 // One classic RK4 step of size h (cuda.c:348-372), in the reference's operation order.
@@ -404,24 +409,24 @@ __device__ CF chi2_fp64(const DevModel& M, const ObsView& o, const double* param
         const double theta = torque ? y[4] : y[1];
         const double psi = torque ? y[5] : y[2];
 
-        double cos_phi = cos(phi);
-        double sin_phi = sin(phi);
+        double cos_phi, sin_phi;
+        sincos(phi, &sin_phi, &cos_phi);
         double N_x = XM_x * cos_phi + YM_x * sin_phi;
         double N_y = YM_y * sin_phi;
         double N_z = XM_z * cos_phi + YM_z * sin_phi;
         double p_x = N_y * M_z - N_z * M_y;
         double p_y = N_z * M_x - N_x * M_z;
         double p_z = N_x * M_y - N_y * M_x;
-        const double cos_theta = cos(theta);
-        const double sin_theta = sin(theta);
+        double cos_theta, sin_theta;
+        sincos(theta, &sin_theta, &cos_theta);
         double a_x = M_x * cos_theta + p_x * sin_theta;
         double a_y = M_y * cos_theta + p_y * sin_theta;
         double a_z = M_z * cos_theta + p_z * sin_theta;
         const double w_x = a_y * N_z - a_z * N_y;
         const double w_y = a_z * N_x - a_x * N_z;
         const double w_z = a_x * N_y - a_y * N_x;
-        const double sin_psi = sin(psi);
-        const double cos_psi = cos(psi);
+        double sin_psi, cos_psi;
+        sincos(psi, &sin_psi, &cos_psi);
         const double b_x = N_x * cos_psi + w_x * sin_psi;
         const double b_y = N_y * cos_psi + w_y * sin_psi;
         const double b_z = N_z * cos_psi + w_z * sin_psi;
@@ -435,10 +440,8 @@ __device__ CF chi2_fp64(const DevModel& M, const ObsView& o, const double* param
         if (bw) {
             // Brightness frame rotated by theta_R, phi_R (cuda.c:475-497), then the
             // black-and-white ball (cuda.c:596-607).
-            cos_phR = cos(AST_P(phi_R));
-            sin_phR = sin(AST_P(phi_R));
-            cos_thR = cos(AST_P(theta_R));
-            sin_thR = sin(AST_P(theta_R));
+            sincos(AST_P(phi_R), &sin_phR, &cos_phR);
+            sincos(AST_P(theta_R), &sin_thR, &cos_thR);
             N_x = b_x * cos_phR + c_x * sin_phR;
             N_y = b_y * cos_phR + c_y * sin_phR;
             N_z = b_z * cos_phR + c_z * sin_phR;

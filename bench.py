@@ -160,7 +160,25 @@ def sample_vectors(model, n, seed, reopt=0):
     return np.array(out)
 
 
-def cpu_baseline(model, obs, seconds=15.0):
+def workload_vectors(model, n, seed, params_true=None, radius=0.02):
+    """Parameter vectors of the workload: from the fit's prior, or -- for NUDGE, which the
+    reference runs as a re-optimisation -- jittered by up to `radius` in every dimensionless
+    coordinate around the true model."""
+    from asteroid_gb300 import api
+
+    if params_true is None or not model.flags & api.NUDGE:
+        return sample_vectors(model, n, seed)
+    rng = np.random.default_rng(seed)
+    x0 = api.params2x(model, params_true)
+    out = []
+    while len(out) < n:
+        p = api.x2params(model, x0 + rng.uniform(-radius, radius, model.n_params), reopt=1)
+        if p is not None:
+            out.append(p)
+    return np.array(out)
+
+
+def cpu_baseline(model, obs, seconds=15.0, params_true=None):
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle as O
 
@@ -168,12 +186,12 @@ def cpu_baseline(model, obs, seconds=15.0):
 
     build.build_oracle()
     threads = O.max_threads()
-    P = sample_vectors(model, 8 * threads, seed=99)
+    P = workload_vectors(model, 8 * threads, 99, params_true)
     t0 = time.perf_counter()
     O.chi2_batch(model, obs, P[: threads], threads=threads)  # warm
     per = (time.perf_counter() - t0) / 1.0
     n = max(threads, int(seconds / max(per, 1e-6) * threads))
-    P = sample_vectors(model, n, seed=100)
+    P = workload_vectors(model, n, 100, params_true)
     t0 = time.perf_counter()
     O.chi2_batch(model, obs, P, threads=threads)
     dt = time.perf_counter() - t0
@@ -181,16 +199,26 @@ def cpu_baseline(model, obs, seconds=15.0):
             "sample": f"{n} parameter vectors of the workload's object, oracle chi2one restatement, OpenMP"}
 
 
-def run_fit_steps(eng, precision, n_chains, group, evals_cap, budget, warmup, steps, seed, stream_events):
-    """Warm-up + timed resumable launches; returns (evals, ms, fits, launches)."""
-    eng.fit_begin(n_chains=n_chains, group_size=group, seed=seed, precision=precision, evals_cap=evals_cap)
+def run_fit_steps(eng, precision, n_chains, group, evals_cap, budget, warmup, steps, seed, stream_events,
+                  reopt=False, params0=None, target_s=1.5):
+    """Warm-up + timed resumable launches; returns (evals, ms, fits, launches, budget).  With
+    budget 0 the first warm-up launch (2 evaluations per slot) calibrates the budget to about
+    target_s of device time per step."""
+    eng.fit_begin(n_chains=n_chains, group_size=group, seed=seed, precision=precision, evals_cap=evals_cap,
+                  reopt=reopt, params0=params0)
+    if budget <= 0:
+        t0 = time.perf_counter()
+        eng.fit_step(2)
+        dt = time.perf_counter() - t0
+        budget = max(1, int(round(2 * target_s / max(dt, 1e-3))))
+        warmup = max(0, warmup - 1)
     for _ in range(warmup):
         eng.fit_step(budget)
     e0, f0 = eng.fit_counters()
     ms, launches = stream_events(lambda: [eng.fit_step(budget) for _ in range(steps)])
     e1, f1 = eng.fit_counters()
     eng.fit_end()
-    return e1 - e0, ms, f1 - f0, steps
+    return e1 - e0, ms, f1 - f0, steps, budget
 
 
 def main():
@@ -206,6 +234,8 @@ def main():
     ap.add_argument("--budget-fp64", type=int, default=0)
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--profile", action="store_true", help="only the fit launches (for ncu)")
     args = ap.parse_args()
 
     world, rank, local, dist = dist_setup()
@@ -223,7 +253,7 @@ def main():
         s = synth.generate(args.config, tmp, vmod_fn=lambda m, o, p: O.model_curve(m, o, p))
         build.build_oracle()
         threads = O.max_threads()
-        P = sample_vectors(s.model, threads, seed=5)
+        P = workload_vectors(s.model, threads, 5, s.params_true)
         O.chi2_batch(s.model, s.obs, P, threads=threads)
         for _ in range(args.warmup):
             O.chi2_batch(s.model, s.obs, P, threads=threads)
@@ -231,7 +261,7 @@ def main():
         O.chi2_batch(s.model, s.obs, P, threads=threads)
         per_step = 10.0
         n = max(threads, int(per_step / max(time.perf_counter() - t0, 1e-6) * threads))
-        P = sample_vectors(s.model, n, seed=6)
+        P = workload_vectors(s.model, n, 6, s.params_true)
         times = []
         for _ in range(args.steps):
             t0 = time.perf_counter()
@@ -280,27 +310,40 @@ def main():
     flops, trans = algorithmic_flops(obs, model)
     seed = 1234 + 7919 * rank
 
-    # Budgets: about one second of device time per step at the expected rates.
-    slots_guess = 152 * 256
-    b_mixed = args.budget_mixed or max(1, int(1.0 * 2.0e6 / slots_guess * 1.0e4 / max(n_rk4, 1)))
-    b_fp64 = args.budget_fp64 or max(1, int(1.0 * 1.5e5 / slots_guess * 1.25e4 / max(n_rk4, 1)))
+    # NUDGE is the reference's Stage-Three option, run with -reopt from a good model
+    # (README.md:88-103): chains start around the true model.  From random starts nearly every
+    # evaluation would take the "more than M_MAX model minima" early exit (cuda.c:738-742).
+    reopt = bool(model.flags & api.NUDGE)
+    p0 = s.params_true if reopt else None
+    main_prec = api.PREC_FP64 if args.precision == "fp64" else api.PREC_MIXED
+
+    if args.profile:
+        # Only the fit launches of one precision (the command profiled under ncu).
+        ev, ms, _, launches, b = run_fit_steps(eng, main_prec, args.chains, 256, args.evals_cap, args.budget_mixed,
+                                               args.warmup, args.steps, seed, timed, reopt, p0)
+        print(json.dumps({"profile": args.precision, "evals": ev, "ms": ms, "evals_per_s": ev / (ms * 1e-3),
+                          "budget": b, "slots": eng.fit_slots()}))
+        eng.close()
+        return
 
     with Clocks(local) as clk:
-        ev_m, ms_m, fits_m, launches_m = run_fit_steps(eng, api.PREC_MIXED, args.chains, 256, args.evals_cap, b_mixed,
-                                                       args.warmup, args.steps, seed, timed)
+        ev_m, ms_m, fits_m, launches_m, b_mixed = run_fit_steps(
+            eng, api.PREC_MIXED, args.chains, 256, args.evals_cap, args.budget_mixed, args.warmup, args.steps, seed,
+            timed, reopt, p0)
     ms_m = max_over_ranks(dist, ms_m)
     ev_m_all = sum_over_ranks(dist, ev_m)
     value = ev_m_all / (ms_m * 1e-3)
 
     fp64 = None
     if not args.skip_fp64:
-        ev_d, ms_d, _, _ = run_fit_steps(eng, api.PREC_FP64, args.chains, 256, args.evals_cap, b_fp64,
-                                         max(1, args.warmup // 2 + 1), max(2, args.steps // 2), seed, timed)
+        ev_d, ms_d, _, _, b_fp64 = run_fit_steps(eng, api.PREC_FP64, args.chains, 256, args.evals_cap,
+                                                 args.budget_fp64, max(1, args.warmup // 2 + 1),
+                                                 max(2, args.steps // 2), seed, timed, reopt, p0)
         ms_d = max_over_ranks(dist, ms_d)
         fp64 = sum_over_ranks(dist, ev_d) / (ms_d * 1e-3)
 
     # Accuracy of the mixed path against FP64 on sampled vectors and on the truth.
-    P = np.vstack([sample_vectors(model, 2047, seed=11 + rank), s.params_true[None, :]])
+    P = np.vstack([workload_vectors(model, 2047, 11 + rank, s.params_true), s.params_true[None, :]])
     c64, _ = eng.eval(P, api.PREC_FP64)
     c32, _ = eng.eval(P, api.PREC_MIXED)
     # Conditioning on the FP64 path itself: chi^2 after a one-ulp move of every parameter.
@@ -316,7 +359,7 @@ def main():
 
     # End to end through the C ABI with host buffers: ast_eval_batch, copies included.
     B = 16384
-    Pe = sample_vectors(model, B, seed=21 + rank)
+    Pe = workload_vectors(model, B, 21 + rank, s.params_true)
     eng.eval(Pe[:256], api.PREC_MIXED)
     t0 = time.perf_counter()
     e2e_steps = 2
@@ -328,7 +371,7 @@ def main():
     peak32 = api.probe_peak("fp32", local)
     peak64 = api.probe_peak("fp64", local)
     achieved = flops * value / 1e9 / max(world, 1)
-    cpu = cpu_baseline(model, obs, args.cpu_seconds) if (rank == 0 and world == 1) else None
+    cpu = cpu_baseline(model, obs, args.cpu_seconds, s.params_true) if (rank == 0 and world == 1) else None
     clocks = clk.summary()
 
     if rank == 0:
@@ -338,8 +381,9 @@ def main():
             "vs_baseline": None, "dtype": "f32 rhs/brightness + f64 state (mixed)", "data": "synthetic",
             "config": {"workload": f"{args.config}: {obs.n_data} points, {obs.n_filters} filters, "
                                    f"{api.flag_names(model.flags)}, TIME_STEP {model.time_step}, "
-                                   f"{args.chains} chains x {args.evals_cap} evals; timed slice of "
-                                   f"{b_mixed} evals/slot/step", "chains_per_gpu": args.chains,
+                                   f"{args.chains} chains x {args.evals_cap} evals"
+                                   f"{' re-optimised from the true model (Stage Three, -reopt)' if reopt else ''}; "
+                                   f"timed slice of {b_mixed} evals/slot/step", "chains_per_gpu": args.chains,
                        "n_data": obs.n_data, "rk4_steps_per_eval": n_rk4, "parallelism": f"replicas x{world}",
                        "l2": "flushed before every timed region (256 MB write); simplex state ~100 MB, obs in smem"},
             "fits_per_s": value / args.evals_cap,

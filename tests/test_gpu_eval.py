@@ -20,9 +20,10 @@ RTOL_FP64 = 1e-9
 COND_LIMIT = 1e-10
 
 
-def well_conditioned(oracle_mod, model, obs, P):
+def well_conditioned(oracle_mod, model, obs, P, return_cond=False):
     """Mask of vectors whose oracle chi^2 (in FP64, CHI_FLOAT = double) moves by at most
-    COND_LIMIT when every parameter is moved by one ulp, for three random sign patterns."""
+    COND_LIMIT when every parameter is moved by one ulp, for three random sign patterns
+    (and, with return_cond, that largest relative move per vector)."""
     acc_model = model
     if not model.flags & api.ACC:
         acc_model = api.make_model(model.flags | api.ACC, model.time_step, (2.0, 4800.0))
@@ -35,7 +36,8 @@ def well_conditioned(oracle_mod, model, obs, P):
         b, _ = oracle_mod.chi2_batch(acc_model, obs, Q)
         with np.errstate(invalid="ignore", divide="ignore"):
             worst = np.maximum(worst, np.abs(a - b) / np.abs(a))
-    return np.isfinite(a) & np.isfinite(worst) & (worst <= COND_LIMIT)
+    mask = np.isfinite(a) & np.isfinite(worst) & (worst <= COND_LIMIT)
+    return (mask, worst) if return_cond else mask
 
 
 def _vectors(model, n, seed, reopt=0, resolved=True):

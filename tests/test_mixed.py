@@ -36,11 +36,9 @@ def test_mixed_within_1e6_of_fp64(gpu, oracle_mod, synth_objects, name):
     print(f"{name}: {both.sum()} vectors, median {np.median(rel):.2e}, p99 {np.quantile(rel, 0.99):.2e}, "
           f"max {rel.max():.2e}, <= {bar}: {frac:.4f}, NUDGE flips {flips}")
     assert rel[-1] <= bar, f"true model: {rel[-1]:.3e}"
-    if s.model.flags & api.NUDGE:
-        assert frac >= 0.97 and flips <= 0.03 * ok.sum()
-    else:
-        assert frac >= 0.99, f"only {frac:.4f} within {bar}"
-    assert np.median(rel) <= 1e-7
+    assert frac >= 0.99, f"only {frac:.4f} within {bar}"
+    assert flips <= 0.01 * ok.sum()
+    assert np.median(rel) <= 2e-7
 
 
 def test_mixed_fit_finds_same_minimum(gpu, synth_objects):
