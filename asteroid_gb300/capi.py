@@ -139,6 +139,9 @@ SIGNATURES = {
     "ast_fit_begin": (C.c_int, [_P, C.POINTER(FitCfg)]),
     "ast_fit_step": (C.c_int, [_P, C.c_int64, C.POINTER(C.c_int32), C.c_void_p]),
     "ast_fit_end": (C.c_int, [_P, C.POINTER(FitOut)]),
+    "ast_fit_noalloc": (C.c_int, [C.POINTER(Model), C.POINTER(ObsSet), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                  C.c_void_p, C.c_void_p, C.POINTER(FitCfg), C.c_void_p, C.c_void_p, C.c_void_p,
+                                  C.c_void_p]),
     "ast_fit_slots": (C.c_int64, [_P]),
     "ast_fit_counters": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "ast_stream": (C.c_void_p, [_P]),

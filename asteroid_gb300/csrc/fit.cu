@@ -697,3 +697,214 @@ extern "C" int ast_fit(ast_ctx* c, const ast_fit_cfg* cfg, ast_fit_out* out)
     }
     return ast_fit_end(c, out);
 }
+
+// ==================================================================================== no-alloc fit
+//
+// ast_fit_noalloc: the same simplex search for callers that cannot allocate device memory --
+// code running inside a host framework that owns every allocation through its own pool, or a
+// process whose memory is reserved up front and must not grow.  Inputs and outputs are the
+// caller's device buffers; everything else the search needs (the observation block, the chain
+// state, per-chain and per-group results, counters) lives in one file-scope device array of
+// AST_NOALLOC_SCRATCH_BYTES, which every GPU that loads this library holds until the process
+// exits.  Nothing here calls cudaMalloc, cudaFree or an allocating library routine.
+//
+// The array is shared by all calls and keeps the last call's contents; each call re-initialises
+// what must start at zero.  Calls whose work overlaps on a GPU (two streams, two threads) race on
+// the array.  The first call on a device looks up the array's device address with
+// cudaGetSymbolAddress with that device current; make that first call before any stream capture.
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[AST_NOALLOC_SCRATCH_BYTES];
+
+namespace ast {
+__global__ void prep_obs_kernel(DevModel M, char* base, ObsLayout L, int64_t n);
+
+template <class CF>
+struct StartPoint {
+    CF x[AST_MAX_PARAMS];
+};
+
+// Every group's stage-0 start point (the -m model, as x) written by value.
+template <class CF>
+__global__ void noalloc_fill_groups_kernel(CF* group_x, int64_t groups, int N, StartPoint<CF> p)
+{
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k < groups * N) group_x[k] = p.x[k % N];
+}
+
+// Copy the caller's observation arrays into the SoA block in scratch (E, S only without INTERP).
+__global__ void noalloc_pack_kernel(char* base, ObsLayout L, int64_t n, const double* mjd, const float* v,
+                                    const float* w, const int32_t* filt, const double* e_unit, const double* s_unit)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    ((double*)(base + L.off_t))[i] = mjd[i];
+    ((float*)(base + L.off_v))[i] = v[i];
+    ((float*)(base + L.off_w))[i] = w[i];
+    ((int32_t*)(base + L.off_f))[i] = filt[i];
+    if (e_unit && s_unit) {
+        double* ex = (double*)(base + L.off_e);
+        double* sx = (double*)(base + L.off_s);
+        for (int k = 0; k < 3; k++) {
+            ex[k * n + i] = e_unit[3 * i + k];
+            sx[k * n + i] = s_unit[3 * i + k];
+        }
+    }
+}
+}  // namespace ast
+
+static void* g_noalloc_ptr[64];
+
+// Bytes of scratch a call needs (the layout of fit_alloc, with the call's own sizes).
+static int64_t noalloc_layout(int64_t S, int64_t C, int64_t G, int N, int NF, int cfb, int64_t obs_bytes,
+                              int64_t* off /* [20] */)
+{
+    auto al = [](int64_t v) { return (v + 255) / 256 * 256; };
+    int64_t o = 0, k = 0;
+    off[k++] = o; o += al(obs_bytes);
+    off[k++] = o; o += al(S * (N + 1) * N * cfb);   // x
+    off[k++] = o; o += al(S * (N + 1) * cfb);       // f
+    off[k++] = o; o += al(S * (N + 1));             // ind
+    off[k++] = o; o += al(S * N * cfb);             // x0
+    off[k++] = o; o += al(S * N * cfb);             // xr
+    off[k++] = o; o += al(S * cfb);                 // fr
+    off[k++] = o; o += al(S * 4);                   // st
+    off[k++] = o; o += al(S * 4);                   // it
+    off[k++] = o; o += al(S * 4);                   // ev
+    off[k++] = o; o += al(S * 8);                   // chain
+    off[k++] = o; o += al(S * NF * 8);              // dv
+    off[k++] = o; o += al(C * 8);                   // chain_f
+    off[k++] = o; o += al(C * N * cfb);             // chain_x
+    off[k++] = o; o += al(C * NF * 8);              // chain_dv
+    off[k++] = o; o += al(G * N * cfb);             // group_x
+    off[k++] = o; o += al(8 * 8);                   // counters
+    return o;
+}
+
+template <class CF, int PREC>
+static int noalloc_run(const DevModel& dm, char* base, const int64_t* off, const ObsLayout& L, const ast_fit_cfg* cfg,
+                       int64_t S, int64_t slots, int tpb, int ctas, size_t smem, double* d_best_f, double* d_best_params,
+                       double* d_best_dv, cudaStream_t s)
+{
+    const int N = dm.n_params, NF = dm.n_filters;
+    const int64_t C = cfg->n_chains, G = C / cfg->group_size;
+    FitView<CF> V;
+    V.x = (CF*)(base + off[1]); V.f = (CF*)(base + off[2]); V.ind = (uint8_t*)(base + off[3]);
+    V.x0 = (CF*)(base + off[4]); V.xr = (CF*)(base + off[5]); V.fr = (CF*)(base + off[6]);
+    V.st = (int32_t*)(base + off[7]); V.it = (int32_t*)(base + off[8]); V.ev = (int32_t*)(base + off[9]);
+    V.chain = (int64_t*)(base + off[10]); V.dv = (double*)(base + off[11]);
+    V.chain_f = (double*)(base + off[12]); V.chain_x = (CF*)(base + off[13]); V.chain_dv = (double*)(base + off[14]);
+    V.group_x = (CF*)(base + off[15]); V.ctr = (unsigned long long*)(base + off[16]);
+    V.S = S; V.n_slots = slots; V.n_chains = C; V.group_size = cfg->group_size;
+    V.seed = cfg->seed; V.evals_cap = cfg->evals_cap; V.steps_cap = cfg->steps_cap > 0 ? cfg->steps_cap : 5000;
+    V.reopt = cfg->reopt ? 1 : 0;
+    // What must start at zero: counters, slot state, the chains' last delta_V.
+    AST_CUDA(cudaMemsetAsync(V.ctr, 0, 8 * 8, s));
+    reset_slots_kernel<<<(unsigned)((S + 255) / 256), 256, 0, s>>>(V.chain, V.st, V.it, V.ev, V.dv, S, NF);
+    AST_CUDA(cudaGetLastError());
+    AST_CUDA(cudaMemsetAsync(V.chain_dv, 0, sizeof(double) * C * NF, s));
+    if (cfg->reopt) {
+        // Every group starts from params2x of the -m model (cuda.c:1409-1416).
+        StartPoint<CF> p;
+        params2x<CF>(dm, cfg->params0, p.x);
+        noalloc_fill_groups_kernel<CF><<<(unsigned)((G * N + 255) / 256), 256, 0, s>>>(V.group_x, G, N, p);
+        AST_CUDA(cudaGetLastError());
+    }
+    for (int32_t stage = 0; stage < cfg->n_stages; stage++) {
+        V.stage = stage;
+        V.last_stage = stage == cfg->n_stages - 1;
+        fit_kernel<CF, PREC><<<ctas, tpb, smem, s>>>(dm, base + off[0], L, smem ? 1 : 0, V, INT64_MAX);
+        AST_CUDA(cudaGetLastError());
+        unsigned long long h[8];
+        AST_CUDA(cudaMemcpyAsync(h, V.ctr, sizeof(h), cudaMemcpyDeviceToHost, s));
+        AST_CUDA(cudaStreamSynchronize(s));
+        if (h[4]) return ast_set_error(AST_E_TIMEOUT, "ast_fit_noalloc: a CTA's shared-memory staging wait ran out");
+        if (h[1] != (unsigned long long)C)
+            return ast_set_error(AST_E_TIMEOUT, "ast_fit_noalloc: stage %d finished %llu of %lld chains", stage, h[1],
+                                 (long long)C);
+        group_best_kernel<CF><<<(unsigned)G, 256, 0, s>>>(dm, V, d_best_f, d_best_params, d_best_dv);
+        AST_CUDA(cudaGetLastError());
+        V.reopt = 1;
+        unsigned long long z[2] = {0, 0};
+        AST_CUDA(cudaMemcpyAsync(V.ctr, z, sizeof(z), cudaMemcpyHostToDevice, s));
+    }
+    AST_CUDA(cudaStreamSynchronize(s));
+    return AST_OK;
+}
+
+extern "C" int ast_fit_noalloc(const ast_model* model, const ast_obs_set* obs, const double* d_mjd, const float* d_v,
+                               const float* d_w, const int32_t* d_filter, const double* d_e_unit,
+                               const double* d_s_unit, const ast_fit_cfg* cfg, double* d_best_f,
+                               double* d_best_params, double* d_best_dv, void* stream)
+{
+    if (!model || !obs || !cfg || !d_mjd || !d_v || !d_w || !d_filter || !d_best_f || !d_best_params || !d_best_dv)
+        return ast_set_error(AST_E_INVALID, "ast_fit_noalloc: NULL argument");
+    const bool interp = (model->flags & AST_INTERP) != 0;
+    if (!interp && (!d_e_unit || !d_s_unit))
+        return ast_set_error(AST_E_INVALID, "ast_fit_noalloc: E/S unit vectors needed without AST_INTERP");
+    if (obs->n_data <= model->n_params + obs->n_filters || obs->n_data > AST_NOALLOC_MAX_DATA)
+        return ast_set_error(AST_E_TOO_LARGE, "ast_fit_noalloc: n_data %d outside %d..%d", obs->n_data,
+                             model->n_params + obs->n_filters + 1, AST_NOALLOC_MAX_DATA);
+    if (obs->n_filters < 1 || obs->n_filters > AST_MAX_FILTERS)
+        return ast_set_error(AST_E_INVALID, "ast_fit_noalloc: n_filters %d outside 1..%d", obs->n_filters, AST_MAX_FILTERS);
+    if (cfg->n_chains <= 0 || cfg->n_chains > AST_NOALLOC_MAX_CHAINS)
+        return ast_set_error(AST_E_TOO_LARGE, "ast_fit_noalloc: n_chains %lld outside 1..%d (the fixed scratch size)",
+                             (long long)cfg->n_chains, AST_NOALLOC_MAX_CHAINS);
+    if (cfg->group_size <= 0 || cfg->n_chains % cfg->group_size || cfg->n_stages <= 0 ||
+        (cfg->precision != AST_PREC_FP64 && cfg->precision != AST_PREC_MIXED) || (cfg->reopt && !cfg->params0))
+        return ast_set_error(AST_E_INVALID, "ast_fit_noalloc: bad configuration");
+    if ((model->flags & AST_NUDGE) && (obs->n_minima < 1 || obs->n_minima > AST_NOBS_MAX))
+        return ast_set_error(AST_E_INVALID, "ast_fit_noalloc: NUDGE needs 1..%d observed minima", AST_NOBS_MAX);
+    DevModel dm;
+    int rc = build_dev_model(model, obs, &dm);
+    if (rc) return rc;
+    int dev = 0;
+    AST_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return ast_set_error(AST_E_INVALID, "ast_fit_noalloc: device %d", dev);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return ast_set_error(AST_E_CUDA, "ast_fit_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+        g_noalloc_ptr[dev] = p;
+    }
+    char* base = (char*)g_noalloc_ptr[dev];
+    cudaStream_t s = (cudaStream_t)stream;
+    const int N = model->n_params, NF = obs->n_filters;
+    const bool acc = (model->flags & AST_ACC) != 0;
+    const int cfb = acc ? 8 : 4;
+    const ObsLayout L = ObsLayout::make(obs->n_data);
+    // Launch geometry as ast_fit_begin chooses it.
+    int sms = 0, optin = 0;
+    AST_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    AST_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    const size_t smem = (size_t)L.bytes + 1024 <= (size_t)optin ? (size_t)L.bytes : 0;
+    int tpb = cfg->tpb;
+    if (tpb <= 0) {
+        const int64_t per_sm = cfg->n_chains / (sms > 0 ? sms : 1);
+        tpb = 32;
+        while (tpb < 256 && tpb * 2 <= per_sm) tpb *= 2;
+    }
+    if (tpb < 32 || tpb > 256 || (tpb & 31)) return ast_set_error(AST_E_INVALID, "ast_fit_noalloc: tpb must be 32..256");
+    const int64_t need = (cfg->n_chains + tpb - 1) / tpb;
+    const int64_t slots = need * tpb, S = (slots + 31) / 32 * 32;
+    int64_t off[20];
+    const int64_t bytes = noalloc_layout(S, cfg->n_chains, cfg->n_chains / cfg->group_size, N, NF, cfb, L.bytes, off);
+    if (bytes > (int64_t)AST_NOALLOC_SCRATCH_BYTES)
+        return ast_set_error(AST_E_TOO_LARGE, "ast_fit_noalloc: needs %lld scratch bytes, the library holds %lld",
+                             (long long)bytes, (long long)AST_NOALLOC_SCRATCH_BYTES);
+    // Observations: pack into scratch, then the per-interval RK4 steps and INTERP E, S.
+    const int64_t n = obs->n_data;
+    noalloc_pack_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(base + off[0], L, n, d_mjd, d_v, d_w, d_filter,
+                                                                    interp ? nullptr : d_e_unit, interp ? nullptr : d_s_unit);
+    AST_CUDA(cudaGetLastError());
+    prep_obs_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(dm, base + off[0], L, n);
+    AST_CUDA(cudaGetLastError());
+    const int ctas = (int)need;
+    if (acc)
+        return cfg->precision == AST_PREC_FP64
+                   ? noalloc_run<double, AST_PREC_FP64>(dm, base, off, L, cfg, S, slots, tpb, ctas, smem, d_best_f, d_best_params, d_best_dv, s)
+                   : noalloc_run<double, AST_PREC_MIXED>(dm, base, off, L, cfg, S, slots, tpb, ctas, smem, d_best_f, d_best_params, d_best_dv, s);
+    return cfg->precision == AST_PREC_FP64
+               ? noalloc_run<float, AST_PREC_FP64>(dm, base, off, L, cfg, S, slots, tpb, ctas, smem, d_best_f, d_best_params, d_best_dv, s)
+               : noalloc_run<float, AST_PREC_MIXED>(dm, base, off, L, cfg, S, slots, tpb, ctas, smem, d_best_f, d_best_params, d_best_dv, s);
+}

@@ -247,6 +247,28 @@ int ast_fit_begin(ast_ctx* ctx, const ast_fit_cfg* cfg);
 int ast_fit_step(ast_ctx* ctx, int64_t evals_per_slot, int32_t* done, void* stream);
 int ast_fit_end(ast_ctx* ctx, ast_fit_out* out);
 
+/* A fit that allocates nothing (no counterpart in the reference).  For callers that cannot
+ * call cudaMalloc -- code embedded in a host framework that owns every device allocation through
+ * its own pool, or a service whose device memory is reserved at start-up and must not grow.
+ * Inputs are the caller's device arrays (d_mjd, d_v, d_w, d_filter as in ast_obs_set; d_e_unit,
+ * d_s_unit [n_data*3], ignored under AST_INTERP) plus the host struct obs for n_data, n_filters,
+ * the INTERP ephemeris and the NUDGE minima (its array pointers are not read).  Outputs are the
+ * caller's device arrays d_best_f[groups], d_best_params[groups*n_params],
+ * d_best_dv[groups*n_filters], with ast_fit's meaning.  All other state lives in one
+ * file-scope device array of AST_NOALLOC_SCRATCH_BYTES (14 MiB) that every GPU loading the
+ * library holds until the process exits; sizes above AST_NOALLOC_MAX_CHAINS chains or
+ * AST_NOALLOC_MAX_DATA observations are rejected with AST_E_TOO_LARGE.  Stream-ordered on
+ * `stream` (NULL = legacy default stream); returns when the fit is complete.  Every call shares
+ * the array: calls that overlap on a GPU race.  The first call on a device looks up the array's
+ * address (cudaGetSymbolAddress) with that device current; make it before any stream capture. */
+#define AST_NOALLOC_MAX_CHAINS 4096
+#define AST_NOALLOC_MAX_DATA 4096
+#define AST_NOALLOC_SCRATCH_BYTES (14u << 20)
+int ast_fit_noalloc(const ast_model* model, const ast_obs_set* obs, const double* d_mjd, const float* d_v,
+                    const float* d_w, const int32_t* d_filter, const double* d_e_unit, const double* d_s_unit,
+                    const ast_fit_cfg* cfg, double* d_best_f, double* d_best_params, double* d_best_dv,
+                    void* stream);
+
 /* Number of chain slots (persistent threads) the fit kernel of this context runs. */
 int64_t ast_fit_slots(ast_ctx* ctx);
 
