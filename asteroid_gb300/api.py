@@ -255,7 +255,8 @@ class Engine:
         check(self.lib.ast_model_curve(self.ctx, dptr(p), dptr(out)), "ast_model_curve")
         return out
 
-    def _cfg(self, n_chains, group_size, n_stages, seed, reopt, params0, precision, evals_cap, steps_cap, tpb):
+    def _cfg(self, n_chains, group_size, n_stages, seed, reopt, params0, precision, evals_cap, steps_cap, tpb,
+             min_ctas_per_sm=0, stage_obs=0):
         cfg = capi.FitCfg()
         cfg.seed = int(seed) & ((1 << 64) - 1)
         cfg.n_chains = int(n_chains)
@@ -266,6 +267,8 @@ class Engine:
         cfg.evals_cap = int(evals_cap)
         cfg.steps_cap = int(steps_cap)
         cfg.tpb = int(tpb)
+        cfg.min_ctas_per_sm = int(min_ctas_per_sm)
+        cfg.stage_obs = int(stage_obs)
         self._p0 = None
         if reopt:
             self._p0 = np.ascontiguousarray(params0, dtype=np.float64)
@@ -273,9 +276,9 @@ class Engine:
         return cfg
 
     def fit_begin(self, n_chains=56 * 256, group_size=256, n_stages=1, seed=1, reopt=False, params0=None,
-                  precision=PREC_FP64, evals_cap=0, steps_cap=0, tpb=0):
+                  precision=PREC_FP64, evals_cap=0, steps_cap=0, tpb=0, min_ctas_per_sm=0, stage_obs=0):
         self._fitcfg = self._cfg(n_chains, group_size, n_stages, seed, reopt, params0, precision, evals_cap,
-                                 steps_cap, tpb)
+                                 steps_cap, tpb, min_ctas_per_sm, stage_obs)
         check(self.lib.ast_fit_begin(self.ctx, C.byref(self._fitcfg)), "ast_fit_begin")
 
     def fit_step(self, evals_per_slot: int = 0, stream: int = 0) -> bool:
@@ -292,6 +295,12 @@ class Engine:
     def fit_slots(self) -> int:
         return int(self.lib.ast_fit_slots(self.ctx))
 
+    def fit_launch(self) -> dict:
+        """Launch geometry of the current fit: CTA size, CTAs, register budget, shared bytes."""
+        v = [C.c_int32(0) for _ in range(4)]
+        check(self.lib.ast_fit_launch(self.ctx, *[C.byref(x) for x in v]), "ast_fit_launch")
+        return dict(tpb=v[0].value, ctas=v[1].value, min_ctas_per_sm=v[2].value, smem=v[3].value)
+
     def fit_end(self) -> FitResult:
         cfg = self._fitcfg
         G = cfg.n_chains // cfg.group_size
@@ -307,9 +316,10 @@ class Engine:
         return res
 
     def fit(self, n_chains=56 * 256, group_size=256, n_stages=1, seed=1, reopt=False, params0=None,
-            precision=PREC_FP64, evals_cap=0, steps_cap=0, tpb=0) -> FitResult:
+            precision=PREC_FP64, evals_cap=0, steps_cap=0, tpb=0, min_ctas_per_sm=0, stage_obs=0) -> FitResult:
         """setup_kernel + chi2_gpu + result copies for one pass (asteroid.c:626-759)."""
-        self.fit_begin(n_chains, group_size, n_stages, seed, reopt, params0, precision, evals_cap, steps_cap, tpb)
+        self.fit_begin(n_chains, group_size, n_stages, seed, reopt, params0, precision, evals_cap, steps_cap, tpb,
+                       min_ctas_per_sm, stage_obs)
         while not self.fit_step(0):
             pass
         return self.fit_end()

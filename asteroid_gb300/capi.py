@@ -95,6 +95,8 @@ class FitCfg(C.Structure):
         ("steps_cap", C.c_int32),
         ("tpb", C.c_int32),
         ("params0", C.POINTER(C.c_double)),
+        ("min_ctas_per_sm", C.c_int32),
+        ("stage_obs", C.c_int32),
     ]
 
 
@@ -143,6 +145,7 @@ SIGNATURES = {
                                   C.c_void_p, C.c_void_p, C.POINTER(FitCfg), C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.c_void_p]),
     "ast_fit_slots": (C.c_int64, [_P]),
+    "ast_fit_launch": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "ast_fit_counters": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "ast_stream": (C.c_void_p, [_P]),
     "ast_probe_peak": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_double)]),

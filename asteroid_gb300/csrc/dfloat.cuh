@@ -32,6 +32,13 @@
 #define DF_FMA(a, b, c) __fmaf_rn(a, b, c)
 #define DF_RCP(a) __frcp_rn(a)
 #define DF_BITS(a) __float_as_int(a)
+__device__ __forceinline__ float df_rcp_approx(float a)
+{
+    float r;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(a));
+    return r;
+}
+#define DF_RCP_APPROX(a) df_rcp_approx(a)
 #else
 static inline float df_h_add(float a, float b) { volatile float r = a + b; return r; }
 static inline float df_h_sub(float a, float b) { volatile float r = a - b; return r; }
@@ -43,6 +50,7 @@ static inline int df_h_bits(float a) { int i; memcpy(&i, &a, 4); return i; }
 #define DF_MUL(a, b) df_h_mul(a, b)
 #define DF_FMA(a, b, c) fmaf(a, b, c)
 #define DF_RCP(a) df_h_rcp(a)
+#define DF_RCP_APPROX(a) df_h_rcp(a)
 #define DF_BITS(a) df_h_bits(a)
 #endif
 
@@ -140,6 +148,46 @@ AST_HD df df_div(df x, df y)
     return df_add_f(q, DF_MUL(r2.hi, inv));
 }
 
+// ------------------------------------------------ cheaper forms for the integrator
+//
+// The right-hand side and the Runge-Kutta stage updates need an absolute error of a few u^2
+// (u = 2^-24) of their operands' magnitudes, not a relative error of the result, so they use
+// the sloppy sum (absolute error <= 2u^2 (|x| + |y|), Joldes et al. Alg. 4 analysis), a product
+// without the lo*lo term, and a quotient with a single Newton correction (relative error ~4u^2).
+
+AST_HD df df_sub_fast(df x, df y) { return df_add_fast(x, df_neg(y)); }
+
+// x*y without the lo*lo term (DWTimesDW1 of Joldes et al.).
+AST_HD df df_mul_fast(df x, df y)
+{
+    const df c = two_prod(x.hi, y.hi);
+    const float t = DF_FMA(x.lo, y.hi, DF_FMA(x.hi, y.lo, c.lo));
+    return fast_two_sum(c.hi, t);
+}
+
+// y + c*k in one pass: the exact product of the high words, the cross terms folded into its
+// error, then a sloppy sum.
+AST_HD df df_mad(df y, df c, df k)
+{
+    const float p = DF_MUL(c.hi, k.hi);
+    const float pe = DF_FMA(c.lo, k.hi, DF_FMA(c.hi, k.lo, DF_FMA(c.hi, k.hi, -p)));
+    const df s = two_sum(y.hi, p);
+    const float v = DF_ADD(DF_ADD(y.lo, pe), s.lo);
+    return fast_two_sum(s.hi, v);
+}
+
+// x / y with one Newton correction of the FP32 quotient.  The reciprocal may be the hardware
+// approximation (relative error ~2^-23): the correction removes its error to first order.
+AST_HD df df_div_fast(df x, df y)
+{
+    const float inv = DF_RCP_APPROX(y.hi);
+    const float q1 = DF_MUL(x.hi, inv);
+    // r = x - y*q1: the high part is exact (fma), the rest carries the low words.
+    const float rh = DF_FMA(-y.hi, q1, x.hi);
+    const float r = DF_FMA(-y.lo, q1, DF_ADD(rh, x.lo));
+    return fast_two_sum(q1, DF_MUL(r, inv));
+}
+
 // ---------------------------------------------------------------- sincos
 
 constexpr int kTrigTable = 256;  // table points over one turn
@@ -190,12 +238,15 @@ AST_HD void df_sincos(df a, const float4* __restrict__ table, df* s_out, df* c_o
     const float kb = DF_ADD(DF_MUL(a.hi, inv_step), magic);
     const float k = DF_SUB(kb, magic);
     const int idx = DF_BITS(kb) & (kTrigTable - 1);
-    // e = a - k * (2pi/TABLE), 2pi/TABLE = C1 + C2 + C3 as three floats.
+    // e = a - k * (2pi/TABLE), 2pi/TABLE = C1 + C2 + C3 as three floats.  a.hi - k*C1 is exact
+    // in one fma (Cody-Waite with a fused multiply-add): both are multiples of ulp(C1) = 2^-29
+    // and |a.hi - k*C1| < 2^-5 for |a.hi| <= 65536, so the difference has at most 24 bits.
     const float C1 = 0.02454369328916073f;      // float(2pi/256)
     const float C2 = -6.829904419802801e-10f;   // float(2pi/256 - C1)
     const float C3 = -2.6798820468841904e-17f;  // float(2pi/256 - C1 - C2)
-    df e = df_sub(a, two_prod(k, C1));
-    e = df_sub(e, two_prod(k, C2));
+    const float e0 = DF_FMA(-k, C1, a.hi);
+    df e = two_sum(e0, a.lo);
+    e = df_sub_fast(e, two_prod(k, C2));
     e = df_add_f(e, -DF_MUL(k, C3));
     // sin e = e - e^3/6 (1 - e^2/20 + e^4/840), cos e = 1 - d with d = e^2/2 - e^4/24 (1 - e^2/30).
     const float e1 = e.hi;
@@ -203,17 +254,74 @@ AST_HD void df_sincos(df a, const float4* __restrict__ table, df* s_out, df* c_o
     const float q = DF_MUL(DF_MUL(e2, 1.0f / 6.0f), DF_FMA(e2, DF_FMA(e2, 1.0f / 840.0f, -1.0f / 20.0f), 1.0f));
     // e^3/6 ~ e1^3/6 + e1^2 e.lo / 2: the second term keeps the low word of e in sin e.
     const df sig = df_add_f(e, -DF_FMA(0.5f * e2, e.lo, DF_MUL(e1, q)));  // sin e
-    df h2 = two_prod(e1, e1);                                            // e^2 as a double-float
-    h2.lo = DF_FMA(2.0f * e1, e.lo, h2.lo);
-    h2 = fast_two_sum(h2.hi, h2.lo);
+    // cos e = 1 - e^2/2 + tail as a double-float: 1 - h with h exact to ~u^2.
+    const float h2 = DF_MUL(e1, e1);
+    const float h2l = DF_FMA(2.0f * e1, e.lo, DF_FMA(e1, e1, -h2));
     const float e4 = DF_MUL(e2, e2);
     const float tail = DF_MUL(DF_MUL(e4, 1.0f / 24.0f), DF_FMA(e2, -1.0f / 30.0f, 1.0f));
-    const df d = df_add_f(df{0.5f * h2.hi, 0.5f * h2.lo}, -tail);  // 1 - cos e
+    const df c0 = fast_two_sum(1.0f, -0.5f * h2);  // exact: |h2/2| < 2^-10
+    const df ce = fast_two_sum(c0.hi, DF_ADD(c0.lo, DF_FMA(-0.5f, h2l, tail)));  // cos e
     const float4 T = table[idx];
     const df S{T.x, T.y}, C{T.z, T.w};
-    // sin a = S - S d + C sin e ; cos a = C - C d - S sin e
-    *s_out = df_add_fast(df_sub(S, df_mul(S, d)), df_mul(C, sig));
-    *c_out = df_sub(df_sub(C, df_mul(C, d)), df_mul(S, sig));
+    // sin a = S cos e + C sin e ; cos a = C cos e - S sin e
+    *s_out = df_add_fast(df_mul_fast(S, ce), df_mul_fast(C, sig));
+    *c_out = df_sub_fast(df_mul_fast(C, ce), df_mul_fast(S, sig));
+}
+
+// ------------------------------------------------ sqrt, atan2, log
+
+// sqrt(x), x >= 0: the FP32 root corrected once with the double-float residual.
+AST_HD df df_sqrt(df x)
+{
+    if (!(x.hi > 0.0f)) return df{x.hi == 0.0f ? 0.0f : sqrtf(x.hi), 0.0f};
+    const float s0 = sqrtf(x.hi);
+    const df p = two_prod(s0, s0);
+    const float d = DF_ADD(DF_SUB(DF_SUB(x.hi, p.hi), p.lo), x.lo);
+    return fast_two_sum(s0, DF_MUL(d, DF_MUL(0.5f, DF_RCP_APPROX(s0))));
+}
+
+// atan2(y, x): the FP32 angle t0 corrected by delta = atan((y cos t0 - x sin t0) / (x cos t0 +
+// y sin t0)) ~ the quotient itself (|delta| ~ 1e-7, so the cubic term is far below u^2).
+AST_HD df df_atan2(df y, df x, const float4* __restrict__ table)
+{
+    const float t0 = atan2f(y.hi, x.hi);
+    df s, c;
+    df_sincos(df{t0, 0.0f}, table, &s, &c);
+    const df num = df_sub(df_mul(y, c), df_mul(x, s));
+    const df den = df_add(df_mul(x, c), df_mul(y, s));
+    const float delta = den.hi != 0.0f ? num.hi / den.hi : 0.0f;
+    return two_sum(t0, delta);
+}
+
+// Natural logarithm, x > 0: x = 2^e m with m in [1/sqrt2, sqrt2), log m = 2 atanh(r),
+// r = (m - 1) / (m + 1), |r| <= 0.1716; the series 2r (1 + z/3 + z^2/5 + z^3 p(z)), z = r^2,
+// carries its first three terms as double-floats and the tail p in FP32 (absolute error of the
+// result ~1e-14).
+AST_HD df df_log(df x)
+{
+    int e;
+    float m = frexpf(x.hi, &e);
+    if (m < 0.70710678f) {
+        m = 2.0f * m;
+        e = e - 1;
+    }
+    const float mlo = ldexpf(x.lo, -e);
+    const df num = two_sum(DF_SUB(m, 1.0f), mlo);  // m - 1 is exact for m in [0.5, 2]
+    const df den = df_add_f(df{m, mlo}, 1.0f);
+    const df r = df_div(num, den);
+    const df z = df_mul(r, r);
+    const float zf = z.hi;
+    const float p = DF_FMA(zf, DF_FMA(zf, DF_FMA(zf, DF_FMA(zf, DF_FMA(zf, DF_FMA(zf, 1.0f / 19.0f, 1.0f / 17.0f),
+                                                                         1.0f / 15.0f), 1.0f / 13.0f), 1.0f / 11.0f),
+                                      1.0f / 9.0f), 1.0f / 7.0f);
+    const df C5{0.2f, -2.9802323e-09f};       // 1/5
+    const df C3{0.33333334f, -9.934108e-09f};  // 1/3
+    df w = df_add_f(C5, DF_MUL(zf, p));
+    w = df_add(C3, df_mul(z, w));
+    w = df_add_f(df_mul(z, w), 1.0f);
+    const df lm = df_mul(df{2.0f * r.hi, 2.0f * r.lo}, w);
+    const df LN2{0.6931472f, -1.9046542e-09f};
+    return df_add(df_mul_f(LN2, (float)e), lm);
 }
 
 // Angle reduced to [-pi, pi] as a float (for FP32 sin/cos in the brightness model).

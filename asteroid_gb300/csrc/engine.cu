@@ -15,6 +15,7 @@
 #include "engine.cuh"
 #include "mixed.cuh"
 #include "model.cuh"
+#include "prep.cuh"
 #include "staging.cuh"
 
 namespace ast {
@@ -71,41 +72,12 @@ int build_dev_model(const ast_model* m, const ast_obs_set* obs, DevModel* dm)
 __global__ void prep_obs_kernel(DevModel M, char* base, ObsLayout L, int64_t n)
 {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    double* t = (double*)(base + L.off_t);
-    double* h = (double*)(base + L.off_h);
-    int32_t* nst = (int32_t*)(base + L.off_nst);
-    if (i == 0) {
-        h[0] = 0.0;
-        nst[0] = 0;
-    } else {
-        const double t1 = t[i - 1], t2 = t[i];
-        const int N_steps = (int)((t2 - t1) / M.time_step + 1);
-        h[i] = (t2 - t1) / N_steps;
-        nst[i] = N_steps;
-    }
-    if (M.flags & AST_INTERP) {
-        double* ex = (double*)(base + L.off_e);
-        double* sx = (double*)(base + L.off_s);
-        const double* M0 = M.eph_mjd0;
-        const double ti = t[i];
-        double rr[3];
-        rr[0] = (ti - M0[1]) * (ti - M0[2]) / (M0[0] - M0[1]) / (M0[0] - M0[2]);
-        rr[1] = (ti - M0[0]) * (ti - M0[2]) / (M0[1] - M0[0]) / (M0[1] - M0[2]);
-        rr[2] = (ti - M0[0]) * (ti - M0[1]) / (M0[2] - M0[0]) / (M0[2] - M0[1]);
-        double E_x1 = M.eph_e[0][0] * rr[0] + M.eph_e[0][1] * rr[1] + M.eph_e[0][2] * rr[2];
-        double E_y1 = M.eph_e[1][0] * rr[0] + M.eph_e[1][1] * rr[1] + M.eph_e[1][2] * rr[2];
-        double E_z1 = M.eph_e[2][0] * rr[0] + M.eph_e[2][1] * rr[1] + M.eph_e[2][2] * rr[2];
-        double S_x1 = M.eph_s[0][0] * rr[0] + M.eph_s[0][1] * rr[1] + M.eph_s[0][2] * rr[2];
-        double S_y1 = M.eph_s[1][0] * rr[0] + M.eph_s[1][1] * rr[1] + M.eph_s[1][2] * rr[2];
-        double S_z1 = M.eph_s[2][0] * rr[0] + M.eph_s[2][1] * rr[1] + M.eph_s[2][2] * rr[2];
-        const double E = sqrt(E_x1 * E_x1 + E_y1 * E_y1 + E_z1 * E_z1);
-        E_x1 = E_x1 / E; E_y1 = E_y1 / E; E_z1 = E_z1 / E;
-        const double S = sqrt(S_x1 * S_x1 + S_y1 * S_y1 + S_z1 * S_z1);
-        S_x1 = S_x1 / S; S_y1 = S_y1 / S; S_z1 = S_z1 / S;
-        ex[i] = E_x1; ex[n + i] = E_y1; ex[2 * n + i] = E_z1;
-        sx[i] = S_x1; sx[n + i] = S_y1; sx[2 * n + i] = S_z1;
-    }
+    if (i < n) prep_obs_point(M, base, L, n, i);
+}
+
+__global__ void prep_sums_kernel(DevModel M, char* base, ObsLayout L, int64_t n)
+{
+    if (blockIdx.x == 0 && threadIdx.x == 0) prep_obs_sums(M, base, L, n);
 }
 
 // One thread per parameter vector; the block's observations are staged into shared memory.
@@ -256,6 +228,8 @@ extern "C" int ast_prepare(const ast_model* model, const ast_obs_set* obs, int32
     }
     AST_CUDA(cudaMemcpyAsync(c->d_obs, img.data(), (size_t)c->layout.bytes, cudaMemcpyHostToDevice, c->stream));
     prep_obs_kernel<<<(unsigned)((n + 127) / 128), 128, 0, c->stream>>>(c->dm, (char*)c->d_obs, c->layout, n);
+    AST_CUDA(cudaGetLastError());
+    prep_sums_kernel<<<1, 32, 0, c->stream>>>(c->dm, (char*)c->d_obs, c->layout, n);
     AST_CUDA(cudaGetLastError());
     AST_CUDA(cudaStreamSynchronize(c->stream));
     *out = c;

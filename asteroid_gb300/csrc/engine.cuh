@@ -55,8 +55,8 @@ struct FitRun {
     int64_t n_evals = 0, n_fits = 0;
     double kernel_ms = 0;
     int tpb = 256, ctas = 0;
-    size_t smem = 0;
-    bool stage_obs_in_smem = true;
+    size_t smem = 0;   // dynamic shared memory of the launch (the observation block, or 0)
+    int minb = 1;      // register budget variant of fit_kernel
 };
 
 }  // namespace ast

@@ -160,9 +160,11 @@ __device__ __forceinline__ CF eval_point(const DevModel& M, const ObsView& o, co
     return chi2_mixed<CF>(M, o, params, dv, trig);
 }
 
-template <class CF, int PREC>
-__global__ void __launch_bounds__(256) fit_kernel(DevModel M, const void* g_obs, ObsLayout L, int use_smem,
-                                                  FitView<CF> V, int64_t budget)
+// MINB: CTAs of 256 threads that must fit on one SM -- 1 lets the compiler use up to 255
+// registers per thread, 2 caps it at 128 (twice the warps per SM, some spilled registers).
+template <class CF, int PREC, int MINB>
+__global__ void __launch_bounds__(256, MINB) fit_kernel(DevModel M, const void* g_obs, ObsLayout L, int use_smem,
+                                                        FitView<CF> V, int64_t budget)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t bar;
@@ -509,11 +511,22 @@ static int fit_alloc(ast_ctx* c, int64_t slots, int64_t chains, int64_t groups, 
 }
 
 template <class CF, int PREC>
-static int fit_launch_cfg(ast_ctx* c, int tpb_req, int64_t n_chains, int* tpb_out, int* ctas_out, size_t* smem_out)
+static decltype(&fit_kernel<CF, PREC, 1>) fit_kernel_ptr(int minb)
 {
-    const size_t smem = ast_obs_smem(c);
-    auto kern = fit_kernel<CF, PREC>;
-    if (smem) AST_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    return minb >= 2 ? fit_kernel<CF, PREC, 2> : fit_kernel<CF, PREC, 1>;
+}
+
+// Launch geometry: CTA size (tpb), register budget (minb) and whether the CTA stages the
+// observations in shared memory.  Staging is dropped when the block would lower the number of
+// CTAs an SM holds (observations are read once per observation, not per RK4 step, so global
+// reads through L1 cost little, while warps per SM decide how well latency is hidden).
+template <class CF, int PREC>
+static int fit_launch_cfg(ast_ctx* c, int tpb_req, int minb_req, int stage_req, int64_t n_chains, FitRun* r)
+{
+    const size_t smem_obs = ast_obs_smem(c);
+    int minb = minb_req >= 2 ? 2 : 1;
+    auto kern = fit_kernel_ptr<CF, PREC>(minb);
+    if (smem_obs) AST_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_obs));
     int tpb = tpb_req;
     if (tpb <= 0) {
         // Enough CTAs to cover every SM before growing the CTA (small chain counts).
@@ -522,16 +535,21 @@ static int fit_launch_cfg(ast_ctx* c, int tpb_req, int64_t n_chains, int* tpb_ou
         while (tpb < 256 && tpb * 2 <= per_sm) tpb *= 2;
     }
     if (tpb < 32 || tpb > 256 || (tpb & 31)) return ast_set_error(AST_E_INVALID, "fit: tpb must be 32..256, multiple of 32");
-    int occ = 1;
-    AST_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, tpb, smem));
-    if (occ < 1) return ast_set_error(AST_E_TOO_LARGE, "fit: kernel does not fit on an SM with %zu B shared memory", smem);
+    int occ_smem = 0, occ_gmem = 0;
+    AST_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_gmem, kern, tpb, 0));
+    if (smem_obs) AST_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_smem, kern, tpb, smem_obs));
+    bool stage = smem_obs != 0 && (stage_req > 0 || (stage_req == 0 && occ_smem >= occ_gmem));
+    if (stage_req > 0 && !smem_obs) stage = false;
+    const int occ = stage ? occ_smem : occ_gmem;
+    if (occ < 1) return ast_set_error(AST_E_TOO_LARGE, "fit: kernel does not fit on an SM");
     int64_t ctas = (int64_t)c->sm_count * occ;
     const int64_t need = (n_chains + tpb - 1) / tpb;
     if (ctas > need) ctas = need;
     if (ctas < 1) ctas = 1;
-    *tpb_out = tpb;
-    *ctas_out = (int)ctas;
-    *smem_out = smem;
+    r->tpb = tpb;
+    r->ctas = (int)ctas;
+    r->smem = stage ? smem_obs : 0;
+    r->minb = minb;
     return AST_OK;
 }
 
@@ -555,12 +573,13 @@ extern "C" int ast_fit_begin(ast_ctx* c, const ast_fit_cfg* cfg)
     r.reopt = cfg->reopt ? 1 : 0;
     const bool acc = (c->model.flags & AST_ACC) != 0;
     const int cfb = acc ? 8 : 4;
+    const int mb = cfg->min_ctas_per_sm, so = cfg->stage_obs;
     if (acc)
-        rc = cfg->precision == AST_PREC_FP64 ? fit_launch_cfg<double, AST_PREC_FP64>(c, cfg->tpb, cfg->n_chains, &r.tpb, &r.ctas, &r.smem)
-                                             : fit_launch_cfg<double, AST_PREC_MIXED>(c, cfg->tpb, cfg->n_chains, &r.tpb, &r.ctas, &r.smem);
+        rc = cfg->precision == AST_PREC_FP64 ? fit_launch_cfg<double, AST_PREC_FP64>(c, cfg->tpb, mb, so, cfg->n_chains, &r)
+                                             : fit_launch_cfg<double, AST_PREC_MIXED>(c, cfg->tpb, mb, so, cfg->n_chains, &r);
     else
-        rc = cfg->precision == AST_PREC_FP64 ? fit_launch_cfg<float, AST_PREC_FP64>(c, cfg->tpb, cfg->n_chains, &r.tpb, &r.ctas, &r.smem)
-                                             : fit_launch_cfg<float, AST_PREC_MIXED>(c, cfg->tpb, cfg->n_chains, &r.tpb, &r.ctas, &r.smem);
+        rc = cfg->precision == AST_PREC_FP64 ? fit_launch_cfg<float, AST_PREC_FP64>(c, cfg->tpb, mb, so, cfg->n_chains, &r)
+                                             : fit_launch_cfg<float, AST_PREC_MIXED>(c, cfg->tpb, mb, so, cfg->n_chains, &r);
     if (rc) return rc;
     const int64_t slots = (int64_t)r.tpb * r.ctas;
     const int64_t groups = cfg->n_chains / cfg->group_size;
@@ -596,7 +615,7 @@ static int fit_step_t(ast_ctx* c, int64_t budget, int32_t* done, cudaStream_t s)
     FitBuffers& b = c->fb;
     FitView<CF> V = make_view<CF>(c);
     AST_CUDA(cudaEventRecord(c->ev0, s));
-    fit_kernel<CF, PREC><<<r.ctas, r.tpb, r.smem, s>>>(c->dm, c->d_obs, c->layout, r.smem ? 1 : 0, V, budget);
+    fit_kernel_ptr<CF, PREC>(r.minb)<<<r.ctas, r.tpb, r.smem, s>>>(c->dm, c->d_obs, c->layout, r.smem ? 1 : 0, V, budget);
     AST_CUDA(cudaGetLastError());
     AST_CUDA(cudaEventRecord(c->ev1, s));
     unsigned long long h[8];
@@ -658,6 +677,16 @@ extern "C" int ast_fit_counters(ast_ctx* c, int64_t* n_evals, int64_t* n_fits)
 
 extern "C" int64_t ast_fit_slots(ast_ctx* c) { return c ? c->fb.slots : 0; }
 
+extern "C" int ast_fit_launch(ast_ctx* c, int32_t* tpb, int32_t* ctas, int32_t* minb, int32_t* smem)
+{
+    if (!c || !c->fb.ctr) return ast_set_error(AST_E_INVALID, "ast_fit_launch: no fit");
+    if (tpb) *tpb = c->run.tpb;
+    if (ctas) *ctas = c->run.ctas;
+    if (minb) *minb = c->run.minb;
+    if (smem) *smem = (int32_t)c->run.smem;
+    return AST_OK;
+}
+
 extern "C" int ast_fit_end(ast_ctx* c, ast_fit_out* out)
 {
     if (!c || !out) return ast_set_error(AST_E_INVALID, "ast_fit_end: NULL argument");
@@ -717,6 +746,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[AST_NOALLOC_SCR
 
 namespace ast {
 __global__ void prep_obs_kernel(DevModel M, char* base, ObsLayout L, int64_t n);
+__global__ void prep_sums_kernel(DevModel M, char* base, ObsLayout L, int64_t n);
 
 template <class CF>
 struct StartPoint {
@@ -812,7 +842,7 @@ static int noalloc_run(const DevModel& dm, char* base, const int64_t* off, const
     for (int32_t stage = 0; stage < cfg->n_stages; stage++) {
         V.stage = stage;
         V.last_stage = stage == cfg->n_stages - 1;
-        fit_kernel<CF, PREC><<<ctas, tpb, smem, s>>>(dm, base + off[0], L, smem ? 1 : 0, V, INT64_MAX);
+        fit_kernel<CF, PREC, 1><<<ctas, tpb, smem, s>>>(dm, base + off[0], L, smem ? 1 : 0, V, INT64_MAX);
         AST_CUDA(cudaGetLastError());
         unsigned long long h[8];
         AST_CUDA(cudaMemcpyAsync(h, V.ctr, sizeof(h), cudaMemcpyDeviceToHost, s));
@@ -898,6 +928,8 @@ extern "C" int ast_fit_noalloc(const ast_model* model, const ast_obs_set* obs, c
                                                                     interp ? nullptr : d_e_unit, interp ? nullptr : d_s_unit);
     AST_CUDA(cudaGetLastError());
     prep_obs_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(dm, base + off[0], L, n);
+    AST_CUDA(cudaGetLastError());
+    prep_sums_kernel<<<1, 32, 0, s>>>(dm, base + off[0], L, n);
     AST_CUDA(cudaGetLastError());
     const int ctas = (int)need;
     if (acc)

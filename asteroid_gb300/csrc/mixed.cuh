@@ -123,53 +123,224 @@ AST_HD double vmod_fp64(const DevModel& M, const ObsView& o, const double* param
                          sin_lambda_p * sin(lambda_p - alpha_p) * log(1.0 / tan(0.5 * lambda_p) / tan(0.5 * (alpha_p - lambda_p)))));
 }
 
-struct DfOde {
-    df mu[6];
-};
+// sin and cos of two double-float angles through one copy of df_sincos (a rolled loop keeps
+// the right-hand side small enough for the instruction cache).
+AST_HD void df_sincos2(df a0, df a1, const float4* tab, df* s0, df* c0, df* s1, df* c1)
+{
+    df sv[2], cv[2];
+#pragma unroll 1
+    for (int q = 0; q < 2; q++) df_sincos(q ? a1 : a0, tab, &sv[q], &cv[q]);
+    *s0 = sv[0]; *c0 = cv[0]; *s1 = sv[1]; *c1 = cv[1];
+}
 
 AST_HD void ode_torque_df(const df* y, df* f, const df* mu, const float4* tab)
 {
     df s5, c5, s4, c4;
-    df_sincos(y[5], tab, &s5, &c5);
-    df_sincos(y[4], tab, &s4, &c4);
-    f[0] = df_add(df_mul(df_mul(mu[0], y[1]), y[2]), mu[3]);
-    f[1] = df_add(df_mul(df_mul(mu[1], y[2]), y[0]), mu[4]);
-    f[2] = df_add(df_mul(df_mul(mu[2], y[0]), y[1]), mu[5]);
-    f[3] = df_div(df_add(df_mul(y[0], s5), df_mul(y[1], c5)), s4);
-    f[4] = df_sub(df_mul(y[0], c5), df_mul(y[1], s5));
-    f[5] = df_sub(y[2], df_mul(f[3], c4));
+    df_sincos2(y[5], y[4], tab, &s5, &c5, &s4, &c4);
+    f[0] = df_add_fast(df_mul_fast(df_mul_fast(mu[0], y[1]), y[2]), mu[3]);
+    f[1] = df_add_fast(df_mul_fast(df_mul_fast(mu[1], y[2]), y[0]), mu[4]);
+    f[2] = df_add_fast(df_mul_fast(df_mul_fast(mu[2], y[0]), y[1]), mu[5]);
+    f[3] = df_div_fast(df_add_fast(df_mul_fast(y[0], s5), df_mul_fast(y[1], c5)), s4);
+    f[4] = df_sub_fast(df_mul_fast(y[0], c5), df_mul_fast(y[1], s5));
+    f[5] = df_sub_fast(y[2], df_mul_fast(f[3], c4));
 }
 
 AST_HD void ode_free_df(const df* y, df* f, const df* mu, const float4* tab)
 {
     df s2, c2, s1, c1;
-    df_sincos(df{2.0f * y[2].hi, 2.0f * y[2].lo}, tab, &s2, &c2);
-    df_sincos(y[1], tab, &s1, &c1);
-    f[0] = df_mul(mu[0], df_sub(mu[1], df_mul(mu[2], c2)));
-    f[1] = df_mul(df_mul(df_mul(mu[0], mu[2]), s1), s2);
-    f[2] = df_mul(c1, df_sub(mu[0], f[0]));
+    df_sincos2(df{2.0f * y[2].hi, 2.0f * y[2].lo}, y[1], tab, &s2, &c2, &s1, &c1);
+    f[0] = df_mul_fast(mu[0], df_sub_fast(mu[1], df_mul_fast(mu[2], c2)));
+    f[1] = df_mul_fast(df_mul_fast(df_mul_fast(mu[0], mu[2]), s1), s2);
+    f[2] = df_mul_fast(c1, df_sub_fast(mu[0], f[0]));
 }
 
+// One RK4 step, y <- y + h/6 K1 + h/3 K2 + h/3 K3 + h/6 K4 with K1..K4 at y, y + h/2 K1,
+// y + h/2 K2, y + h K3 (cuda.c:319-372).  hq = (h, h/2), hw = (h/6, h/3) as double-floats.
+// The four stages run through a single right-hand-side call site (a rolled loop) and the new
+// state is accumulated as the stage derivatives come, so the hot loop is one copy of the
+// right-hand side -- small enough for the instruction cache -- and only one stage derivative
+// is live at a time.  Sums and products are the integrator forms of dfloat.cuh (absolute
+// error a few u^2 of the operands).
 template <int NODE>
-AST_HD void rk4_step_df(df* y, df hh, df h, df h6, const df* mu, const float4* tab)
+AST_HD void rk4_step_df(df* y, float4 hq, float4 hw, const df* mu, const float4* tab)
 {
-    df f[NODE], K1[NODE], K2[NODE], K3[NODE], K4[NODE];
-    if (NODE == 6) ode_torque_df(y, K1, mu, tab); else ode_free_df(y, K1, mu, tab);
+    df f[NODE], K[NODE], yn[NODE];
 #pragma unroll
-    for (int j = 0; j < NODE; j++) f[j] = df_add(y[j], df_mul(hh, K1[j]));
-    if (NODE == 6) ode_torque_df(f, K2, mu, tab); else ode_free_df(f, K2, mu, tab);
+    for (int j = 0; j < NODE; j++) f[j] = y[j];
+#pragma unroll 1
+    for (int st = 0; st < 4; st++) {
+        if (NODE == 6) ode_torque_df(f, K, mu, tab); else ode_free_df(f, K, mu, tab);
+        const df c = st < 2 ? df{hq.z, hq.w} : df{hq.x, hq.y};                    // h/2, h/2, h, h
+        const df wgt = (st == 1 || st == 2) ? df{hw.z, hw.w} : df{hw.x, hw.y};   // h/6, h/3, h/3, h/6
 #pragma unroll
-    for (int j = 0; j < NODE; j++) f[j] = df_add(y[j], df_mul(hh, K2[j]));
-    if (NODE == 6) ode_torque_df(f, K3, mu, tab); else ode_free_df(f, K3, mu, tab);
-#pragma unroll
-    for (int j = 0; j < NODE; j++) f[j] = df_add(y[j], df_mul(h, K3[j]));
-    if (NODE == 6) ode_torque_df(f, K4, mu, tab); else ode_free_df(f, K4, mu, tab);
-#pragma unroll
-    for (int j = 0; j < NODE; j++) {
-        const df s23 = df_add(K2[j], K3[j]);
-        const df s = df_add(df_add(K1[j], K4[j]), df{2.0f * s23.hi, 2.0f * s23.lo});
-        y[j] = df_add(y[j], df_mul(h6, s));
+        for (int j = 0; j < NODE; j++) {
+            yn[j] = df_mad(st == 0 ? y[j] : yn[j], wgt, K[j]);
+            f[j] = df_mad(y[j], c, K[j]);
+        }
     }
+#pragma unroll
+    for (int j = 0; j < NODE; j++) y[j] = yn[j];
+}
+
+// ---------------------------------------------------------------- double-float magnitudes
+//
+// The NUDGE minimum candidates need model magnitudes far more accurate than FP32 (their
+// parabola turns magnitude differences of ~1e-3 mag into the minimum's time).  They are
+// evaluated here in double-float arithmetic on the FP32 pipe, ~1e-13 mag, rather than in FP64,
+// which on GB300 runs at 1/64 of the FP32 rate.
+
+AST_HD df df_dot3(const df* a, const df* b)
+{
+    return df_add(df_add(df_mul(a[0], b[0]), df_mul(a[1], b[1])), df_mul(a[2], b[2]));
+}
+AST_HD void df_cross3(const df* a, const df* b, df* c)
+{
+    c[0] = df_sub(df_mul(a[1], b[2]), df_mul(a[2], b[1]));
+    c[1] = df_sub(df_mul(a[2], b[0]), df_mul(a[0], b[2]));
+    c[2] = df_sub(df_mul(a[0], b[1]), df_mul(a[1], b[0]));
+}
+
+// f(t) = t - (1 - t^2) atanh(t), 0 <= t < 1 (ls_f in double-float): the series
+// t^3 sum_{k>=1} 2 t^(2k-2) / ((2k-1)(2k+1)) below 1/4, the closed form above.
+AST_HD df ls_f_df(df t)
+{
+    const df z = df_mul(t, t);
+    if (t.hi < 0.25f) {
+        const float zf = z.hi;
+        float p = 2.0f / 899.0f;  // k = 15: 2 / (29 * 31)
+        p = DF_FMA(p, zf, 2.0f / 783.0f);
+        p = DF_FMA(p, zf, 2.0f / 675.0f);
+        p = DF_FMA(p, zf, 2.0f / 575.0f);
+        p = DF_FMA(p, zf, 2.0f / 483.0f);
+        p = DF_FMA(p, zf, 2.0f / 399.0f);
+        p = DF_FMA(p, zf, 2.0f / 323.0f);
+        p = DF_FMA(p, zf, 2.0f / 255.0f);
+        p = DF_FMA(p, zf, 2.0f / 195.0f);
+        p = DF_FMA(p, zf, 2.0f / 143.0f);
+        p = DF_FMA(p, zf, 2.0f / 99.0f);
+        p = DF_FMA(p, zf, 2.0f / 63.0f);  // k = 4
+        const df C2{0.057142857f, -3.193106e-10f};  // 2/35
+        const df C1{0.13333334f, -6.9538753e-09f};  // 2/15
+        const df C0{0.6666667f, -1.9868216e-08f};   // 2/3
+        df w = df_add_f(C2, DF_MUL(zf, p));
+        w = df_add(C1, df_mul(z, w));
+        w = df_add(C0, df_mul(z, w));
+        return df_mul(df_mul(z, t), w);
+    }
+    // atanh t = log((1 + t) / (1 - t)) / 2
+    const df at = df_log(df_div(df_add_f(t, 1.0f), df_add_f(df_neg(t), 1.0f)));
+    const df one_m_z = df_add_f(df_neg(z), 1.0f);
+    return df_sub(t, df_mul(one_m_z, df{0.5f * at.hi, 0.5f * at.lo}));
+}
+
+// ls_magnitude_f in double-float: the same cancellation-free Lommel-Seeliger form.
+AST_HD df ls_magnitude_df(const df* Sp, const df* Ep, df ib, df ic, df bc, const float4* tab)
+{
+    const df sv[3] = {df_mul(Sp[0], ib), df_mul(Sp[1], ic), Sp[2]};
+    const df ev[3] = {df_mul(Ep[0], ib), df_mul(Ep[1], ic), Ep[2]};
+    const df hv[3] = {df_mul(df_add(Sp[0], Ep[0]), ib), df_mul(df_add(Sp[1], Ep[1]), ic), df_add(Sp[2], Ep[2])};
+    const df sS = df_sqrt(df_dot3(sv, sv));
+    const df sE = df_sqrt(df_dot3(ev, ev));
+    const df scalar = df_sqrt(df_dot3(hv, hv));
+    df cr[3];
+    df_cross3(sv, ev, cr);
+    const df cn = df_sqrt(df_dot3(cr, cr));
+    const df mu = df_atan2(cn, df_dot3(sv, hv), tab);
+    const df nu = df_atan2(cn, df_dot3(hv, ev), tab);
+    const df eps = df_atan2(cn, df_neg(df_dot3(sv, ev)), tab);
+    df sd, D, s, cd;
+    const df hmn = df_sub(mu, nu);
+    df_sincos(df{0.5f * hmn.hi, 0.5f * hmn.lo}, tab, &sd, &D);
+    df_sincos(df{0.5f * eps.hi, 0.5f * eps.lo}, tab, &s, &cd);
+    const df B = df_mul(df_mul(df{2.0f * D.hi, 2.0f * D.lo}, D), ls_f_df(df_div(s, D)));
+    const df arg = df_mul(df_div(df_mul(df_mul(bc, sS), sE), scalar), B);
+    const df INV_LN10{0.4342945f, -1.010305e-08f};
+    return df_mul_f(df_mul(df_log(arg), INV_LN10), -2.5f);
+}
+
+// Per-evaluation constants of the double-float magnitude: the spin-axis frame (cuda.c:195-217)
+// and the shape or BW_BALL parameters.
+struct DfFrame {
+    df M[3], XM_x, XM_z, YM[3];
+    df ib, ic, bc;
+    df cR, sR, cT, sT, kappa;
+};
+
+// Model magnitude at observation i for the double-float Euler angles ang = (phi, theta, psi):
+// the body frame as in cuda.c:432-473, then ls_magnitude_df or the BW_BALL law (cuda.c:568-580).
+AST_HD double vmod_df(const DevModel& M, const ObsView& o, const DfFrame& F, const df* ang, int i, const float4* tab)
+{
+    df sph, cph, sth, cth, sps, cps;
+    df_sincos(ang[0], tab, &sph, &cph);
+    df_sincos(ang[1], tab, &sth, &cth);
+    df_sincos(ang[2], tab, &sps, &cps);
+    const df N[3] = {df_add(df_mul(F.XM_x, cph), df_mul(F.YM[0], sph)), df_mul(F.YM[1], sph),
+                     df_add(df_mul(F.XM_z, cph), df_mul(F.YM[2], sph))};
+    df p[3];
+    df_cross3(N, F.M, p);
+    df a[3], w[3], b[3], c[3];
+    for (int k = 0; k < 3; k++) a[k] = df_add(df_mul(F.M[k], cth), df_mul(p[k], sth));
+    df_cross3(a, N, w);
+    for (int k = 0; k < 3; k++) b[k] = df_add(df_mul(N[k], cps), df_mul(w[k], sps));
+    df_cross3(a, b, c);
+    const df E[3] = {df_from_double(o.ex[i]), df_from_double(o.ey[i]), df_from_double(o.ez[i])};
+    if (M.flags & AST_BW_BALL) {
+        df Nb[3], pb[3];
+        for (int k = 0; k < 3; k++) Nb[k] = df_add(df_mul(b[k], F.cR), df_mul(c[k], F.sR));
+        df_cross3(Nb, a, pb);
+        for (int k = 0; k < 3; k++) a[k] = df_add(df_mul(a[k], F.cT), df_mul(pb[k], F.sT));
+        const df cz = df_dot3(a, E);
+        const df one_p = df_add_f(cz, 1.0f), one_m = df_add_f(df_neg(cz), 1.0f);
+        const df arg = df_add(df_mul(F.kappa, one_p), df{0.5f * one_m.hi, 0.5f * one_m.lo});
+        const df l10 = df_mul(df_log(df{0.5f * arg.hi, 0.5f * arg.lo}), df{0.4342945f, -1.010305e-08f});
+        return -2.5 * df_to_double(l10);
+    }
+    const df S[3] = {df_from_double(o.sx[i]), df_from_double(o.sy[i]), df_from_double(o.sz[i])};
+    const df Sp[3] = {df_dot3(b, S), df_dot3(c, S), df_dot3(a, S)};
+    const df Ep[3] = {df_dot3(b, E), df_dot3(c, E), df_dot3(a, E)};
+    return df_to_double(ls_magnitude_df(Sp, Ep, F.ib, F.ic, F.bc, tab));
+}
+
+// NUDGE minimum candidates of the mixed path: observation i and the Euler angles at i-2, i-1, i.
+// They are re-evaluated with double-float magnitudes in queue order after the last observation
+// (or when the queue fills).  Deferring them lets the lanes of a warp evaluate their candidates
+// side by side (each lane has its own, at different observations) instead of one observation
+// after another; the queue is long enough (more than the AST_M_MAX minima a model may have)
+// that a flush in the middle of the light curve, which the lanes would take one at a time, is
+// rare.
+constexpr int kNudgeQueue = 32;
+struct NudgeCand {
+    int i;
+    df a[3][3];
+};
+
+// The reference's test and parabola (cuda.c:716-760) on each queued triple, with double-float
+// magnitudes.  Returns false as soon as more than AST_M_MAX minima are found (the model is then
+// rejected exactly as the reference rejects it, only after a few more observations).
+// Not inlined: the magnitude code is cold and large, and one copy serves both call sites.
+static __host__ __device__ __noinline__ bool nudge_flush(const DevModel& M, const ObsView& o, const DfFrame& F,
+                                                         const float4* tab, NudgeCand* cand, int* n_cand, int* Mmin,
+                                                         float* t_mod, float* V_mod)
+{
+    for (int q = 0; q < *n_cand; q++) {
+        const int ic = cand[q].i;
+        const float f0 = (float)vmod_df(M, o, F, cand[q].a[0], ic - 2, tab);
+        const float f1 = (float)vmod_df(M, o, F, cand[q].a[1], ic - 1, tab);
+        const double v2 = vmod_df(M, o, F, cand[q].a[2], ic, tab);
+        if (f1 > f0 && f1 >= v2) {
+            if (++*Mmin > AST_M_MAX) return false;
+            const float t0 = (float)o.t[ic - 2], t1 = (float)o.t[ic - 1];
+            const double ti = o.t[ic];
+            const double a = ((v2 - f1) / (ti - t1) - (f1 - f0) / (t1 - t0)) / (ti - t0);
+            const double b = (f1 - f0) / (t1 - t0) - a * (t1 + t0);
+            const double c = f1 - a * t1 * t1 - b * t1;
+            const int m = *Mmin - 1;
+            t_mod[m] = (float)(-b / 2.0 / a);
+            V_mod[m] = (float)(a * t_mod[m] * t_mod[m] + b * t_mod[m] + c);
+        }
+    }
+    *n_cand = 0;
+    return true;
 }
 
 // Same contract as chi2_fp64 (model.cuh); tab is the shared-memory sin/cos table.
@@ -179,12 +350,14 @@ __host__ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const dou
     const int flags = M.flags;
     const ast_type_ids& T = M.t;
     const int N_data = M.n_data, N_filters = M.n_filters;
-    double sum_y2[AST_MAX_FILTERS], sum_y[AST_MAX_FILTERS], sum_w[AST_MAX_FILTERS];
-    for (int m = 0; m < N_filters; m++) { sum_y2[m] = 0.0; sum_y[m] = 0.0; sum_w[m] = 0.0; }
+    df sum_y2[AST_MAX_FILTERS], sum_y[AST_MAX_FILTERS];
+    for (int m = 0; m < N_filters; m++) { sum_y2[m] = df{0.0f, 0.0f}; sum_y[m] = df{0.0f, 0.0f}; }
     int Mmin = 0;
     float t_mod[AST_M_MAX], V_mod[AST_M_MAX];
     float t_old[2] = {0.f, 0.f}, V_old[2] = {0.f, 0.f};
-    double ang_old[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    df ang_old[2][3] = {};
+    NudgeCand cand[kNudgeQueue];
+    int n_cand = 0;
 
 #define AST_P(tt) params[M.idx[T.tt]]
     // Per-evaluation set-up in FP64.
@@ -238,21 +411,53 @@ __host__ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const dou
         c_ph = (float)((flags & AST_BC) ? AST_P(c) : ct);
     }
     const float ib = 1.0f / b_ph, ic = 1.0f / c_ph;
+    DfFrame F;
+    if (flags & AST_NUDGE) {
+        F.M[0] = df_from_double(M_xd);
+        F.M[1] = df_from_double(M_yd);
+        F.M[2] = df_from_double(M_zd);
+        F.XM_x = df_from_double(M_zd / XMd);
+        F.XM_z = df_from_double(-M_xd / XMd);
+        F.YM[0] = df_from_double(M_yd * (-M_xd / XMd));
+        F.YM[1] = df_from_double(M_zd * (M_zd / XMd) - M_xd * (-M_xd / XMd));
+        F.YM[2] = df_from_double(-M_yd * (M_zd / XMd));
+        if (bw) {
+            F.kappa = df_from_double(AST_P(kappa));
+            F.cR = df_from_double(cos(AST_P(phi_R)));
+            F.sR = df_from_double(sin(AST_P(phi_R)));
+            F.cT = df_from_double(cos(AST_P(theta_R)));
+            F.sT = df_from_double(sin(AST_P(theta_R)));
+        } else {
+            const double bb = (flags & AST_BC) ? AST_P(b) : bt, cc = (flags & AST_BC) ? AST_P(c) : ct;
+            F.ib = df_from_double(1.0 / bb);
+            F.ic = df_from_double(1.0 / cc);
+            F.bc = df_from_double(bb * cc);
+        }
+    }
 
     for (int i = 0; i < N_data; i++) {
         if (i > 0) {
             const int N_steps = o.nst[i];
-            const double hd = o.h[i];
-            const df h = df_from_double(hd), hh = df_from_double(0.5 * hd), h6 = df_from_double(hd / 6.0);
-            if (torque)
-                for (int l = 0; l < N_steps; l++) rk4_step_df<6>(y, hh, h, h6, mu, tab);
-            else
-                for (int l = 0; l < N_steps; l++) rk4_step_df<3>(y, hh, h, h6, mu, tab);
+            const float4 hq = o.hq[i], hw = o.hw[i];
+            // Not unrolled: one copy of the step keeps the hot loop inside the instruction cache.
+            if (torque) {
+#pragma unroll 1
+                for (int l = 0; l < N_steps; l++) rk4_step_df<6>(y, hq, hw, mu, tab);
+            } else {
+#pragma unroll 1
+                for (int l = 0; l < N_steps; l++) rk4_step_df<3>(y, hq, hw, mu, tab);
+            }
         }
+        // The Euler angles enter the right-hand side and the brightness only through sin and
+        // cos, so they are kept reduced to [-pi, pi]: the double-float then resolves the phase
+        // to ~1e-14 rad instead of u^2 of the accumulated angle.
+        const int a0 = torque ? 3 : 0;
+#pragma unroll
+        for (int k = 0; k < 3; k++) y[a0 + k] = df_reduce_2pi(y[a0 + k]);
         float sin_phi, cos_phi, sin_theta, cos_theta, sin_psi, cos_psi;
-        sincosf(df_reduce_f(torque ? y[3] : y[0]), &sin_phi, &cos_phi);
-        sincosf(df_reduce_f(torque ? y[4] : y[1]), &sin_theta, &cos_theta);
-        sincosf(df_reduce_f(torque ? y[5] : y[2]), &sin_psi, &cos_psi);
+        sincosf(DF_ADD(y[a0].hi, y[a0].lo), &sin_phi, &cos_phi);
+        sincosf(DF_ADD(y[a0 + 1].hi, y[a0 + 1].lo), &sin_theta, &cos_theta);
+        sincosf(DF_ADD(y[a0 + 2].hi, y[a0 + 2].lo), &sin_psi, &cos_psi);
         float N_x = XM_x * cos_phi + YM_x * sin_phi;
         float N_y = YM_y * sin_phi;
         float N_z = XM_z * cos_phi + YM_z * sin_phi;
@@ -271,8 +476,8 @@ __host__ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const dou
         const float c_x = a_y * b_z - a_z * b_y;
         const float c_y = a_z * b_x - a_x * b_z;
         const float c_z = a_x * b_y - a_y * b_x;
-        const float E_x1 = (float)o.ex[i], E_y1 = (float)o.ey[i], E_z1 = (float)o.ez[i];
-        const float S_x1 = (float)o.sx[i], S_y1 = (float)o.sy[i], S_z1 = (float)o.sz[i];
+        const float E_x1 = o.efx[i], E_y1 = o.efy[i], E_z1 = o.efz[i];
+        const float S_x1 = o.sfx[i], S_y1 = o.sfy[i], S_z1 = o.sfz[i];
         float Vmod;
         if (bw) {
             N_x = b_x * cos_phR + c_x * sin_phR;
@@ -296,40 +501,36 @@ __host__ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const dou
             Vmod = ls_magnitude_f(Sp_b, Sp_c, Sp_a, Ep_b, Ep_c, Ep_a, ib, ic, b_ph * c_ph);
         }
         {
+            // Residual and weighted sums as double-floats: v - Vmod exactly (TwoSum), products
+            // to ~u^2, sums with the sloppy double-float add (absolute error ~u^2 of the sum).
             const int m = o.f[i];
-            const double yv = (double)o.v[i] - (double)Vmod;
-            const double wi = o.w[i];
-            sum_y2[m] = fma(yv * yv, wi, sum_y2[m]);
-            sum_y[m] = fma(yv, wi, sum_y[m]);
-            sum_w[m] = sum_w[m] + wi;
+            const df yv = two_sum(o.v[i], -Vmod);
+            const df wy = df_mul_f(yv, o.w[i]);
+            sum_y[m] = df_add_fast(sum_y[m], wy);
+            sum_y2[m] = df_add_fast(sum_y2[m], df_mul_fast(wy, yv));
         }
         if (flags & AST_NUDGE) {
             // Model minima near observed minima (cuda.c:716-760).  The detection and the parabola
             // are discontinuous in the magnitudes (the reference even rounds them to float), so an
             // FP32 magnitude is used only to rule a triple out with a margin far above its error;
-            // a candidate triple is re-evaluated in FP64 from the double-float angles and tested
-            // exactly as the reference tests it.
-            const double ang_i[3] = {df_to_double(torque ? y[3] : y[0]), df_to_double(torque ? y[4] : y[1]),
-                                     df_to_double(torque ? y[5] : y[2])};
+            // a candidate triple is queued with its double-float angles and re-evaluated with
+            // double-float magnitudes (nudge_flush), in order, exactly as the reference tests it.
+            const df ang_i[3] = {torque ? y[3] : y[0], torque ? y[4] : y[1], torque ? y[5] : y[2]};
             if (i >= 2) {
                 bool local = false;
                 for (int ii = 0; ii < M.n_min; ii++)
                     if (fabsf(t_old[1] - M.t_min[ii]) < AST_DT_MAX2) local = true;
                 const float margin = 1e-4f;
                 if (local && V_old[1] > V_old[0] - margin && V_old[1] >= Vmod - margin) {
-                    const float f0 = (float)vmod_fp64(M, o, params, ang_old[0], i - 2);
-                    const float f1 = (float)vmod_fp64(M, o, params, ang_old[1], i - 1);
-                    const double v2 = vmod_fp64(M, o, params, ang_i, i);
-                    if (f1 > f0 && f1 >= v2) {
-                        Mmin++;
-                        if (Mmin > AST_M_MAX) return (CF)kHuge;
-                        const double ti = o.t[i];
-                        const double a = ((v2 - f1) / (ti - t_old[1]) - (f1 - f0) / (t_old[1] - t_old[0])) / (ti - t_old[0]);
-                        const double b = (f1 - f0) / (t_old[1] - t_old[0]) - a * (t_old[1] + t_old[0]);
-                        const double c = f1 - a * t_old[1] * t_old[1] - b * t_old[1];
-                        t_mod[Mmin - 1] = (float)(-b / 2.0 / a);
-                        V_mod[Mmin - 1] = (float)(a * t_mod[Mmin - 1] * t_mod[Mmin - 1] + b * t_mod[Mmin - 1] + c);
+                    NudgeCand& q = cand[n_cand];
+                    q.i = i;
+                    for (int k = 0; k < 3; k++) {
+                        q.a[0][k] = ang_old[0][k];
+                        q.a[1][k] = ang_old[1][k];
+                        q.a[2][k] = ang_i[k];
                     }
+                    if (++n_cand == kNudgeQueue && !nudge_flush(M, o, F, tab, cand, &n_cand, &Mmin, t_mod, V_mod))
+                        return (CF)kHuge;
                 }
             }
             const int slot = i < 2 ? i : 1;
@@ -343,13 +544,15 @@ __host__ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const dou
             for (int k = 0; k < 3; k++) ang_old[slot][k] = ang_i[k];
         }
     }
+    if ((flags & AST_NUDGE) && !nudge_flush(M, o, F, tab, cand, &n_cand, &Mmin, t_mod, V_mod)) return (CF)kHuge;
 #undef AST_P
     CF chi2m, chi2a = 0.0;
     CF dv[AST_MAX_FILTERS];
     for (int m = 0; m < N_filters; m++) {
-        chi2m = (CF)(sum_y2[m] - sum_y[m] * sum_y[m] / sum_w[m]);
+        const double sy = df_to_double(sum_y[m]), sy2 = df_to_double(sum_y2[m]), sw = o.sum_w[m];
+        chi2m = (CF)(sy2 - sy * sy / sw);
         chi2a = chi2a + chi2m;
-        dv[m] = (CF)(sum_y[m] / sum_w[m]);
+        dv[m] = (CF)(sy / sw);
     }
     chi2a = chi2a / (CF)(N_data - M.n_params - N_filters);
     if (flags & AST_NUDGE) {

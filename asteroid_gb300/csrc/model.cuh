@@ -59,12 +59,23 @@ struct ObsView {
     const double* sx;
     const double* sy;
     const double* sz;
+    // Derived for the mixed-precision path (prep_obs_point): step sizes as double-floats,
+    // unit vectors rounded to float, per-filter weight sums.
+    const float4* hq;      // (h, h/2)
+    const float4* hw;      // (h/6, h/3)
+    const float* efx;
+    const float* efy;
+    const float* efz;
+    const float* sfx;
+    const float* sfy;
+    const float* sfz;
+    const double* sum_w;   // [AST_MAX_FILTERS]
 };
 
 // Byte layout of the SoA buffer for n observations: every array starts on a 16-byte boundary
 // and the total is a multiple of 16, as the bulk copies into shared memory require.
 struct ObsLayout {
-    int64_t off_t, off_h, off_nst, off_v, off_w, off_f, off_e, off_s, bytes;
+    int64_t off_t, off_h, off_nst, off_v, off_w, off_f, off_e, off_s, off_hq, off_hw, off_ef, off_sf, off_sw, bytes;
     AST_HD static int64_t up16(int64_t x) { return (x + 15) & ~(int64_t)15; }
     AST_HD static ObsLayout make(int64_t n)
     {
@@ -74,6 +85,11 @@ struct ObsLayout {
         L.off_h = o;   o = up16(o + 8 * n);
         L.off_e = o;   o = up16(o + 3 * 8 * n);
         L.off_s = o;   o = up16(o + 3 * 8 * n);
+        L.off_hq = o;  o = up16(o + 16 * n);
+        L.off_hw = o;  o = up16(o + 16 * n);
+        L.off_sw = o;  o = up16(o + 8 * AST_MAX_FILTERS);
+        L.off_ef = o;  o = up16(o + 3 * 4 * n);
+        L.off_sf = o;  o = up16(o + 3 * 4 * n);
         L.off_nst = o; o = up16(o + 4 * n);
         L.off_v = o;   o = up16(o + 4 * n);
         L.off_w = o;   o = up16(o + 4 * n);
@@ -97,6 +113,15 @@ struct ObsLayout {
         o.v = (const float*)(b + off_v);
         o.w = (const float*)(b + off_w);
         o.f = (const int32_t*)(b + off_f);
+        o.hq = (const float4*)(b + off_hq);
+        o.hw = (const float4*)(b + off_hw);
+        o.efx = (const float*)(b + off_ef);
+        o.efy = o.efx + n;
+        o.efz = o.efy + n;
+        o.sfx = (const float*)(b + off_sf);
+        o.sfy = o.sfx + n;
+        o.sfz = o.sfy + n;
+        o.sum_w = (const double*)(b + off_sw);
         return o;
     }
 };
@@ -400,10 +425,13 @@ __device__ CF chi2_fp64(const DevModel& M, const ObsView& o, const double* param
         if (i > 0) {
             const int N_steps = o.nst[i];
             const double h = o.h[i];
-            if (torque)
+            if (torque) {
+#pragma unroll 1
                 for (int l = 0; l < N_steps; l++) rk4_step<6>(y, h, mu);
-            else
+            } else {
+#pragma unroll 1
                 for (int l = 0; l < N_steps; l++) rk4_step<3>(y, h, mu);
+            }
         }
         const double phi = torque ? y[3] : y[0];
         const double theta = torque ? y[4] : y[1];

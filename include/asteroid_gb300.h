@@ -223,6 +223,9 @@ typedef struct ast_fit_cfg {
     int32_t  steps_cap;     /* N_STEPS (asteroid.h:213); 0 = 5000 */
     int32_t  tpb;           /* threads per CTA; 0 = autotuned */
     const double* params0;  /* [n_params] start model for reopt (d_params0) */
+    int32_t  min_ctas_per_sm; /* register budget: 1 (or 0) = up to 255 registers/thread, 2 = 128 */
+    int32_t  stage_obs;     /* observations in shared memory: 1 = always when they fit, -1 = never,
+                                 0 = only when it does not lower the CTAs per SM */
 } ast_fit_cfg;
 
 typedef struct ast_fit_out {
@@ -271,6 +274,12 @@ int ast_fit_noalloc(const ast_model* model, const ast_obs_set* obs, const double
 
 /* Number of chain slots (persistent threads) the fit kernel of this context runs. */
 int64_t ast_fit_slots(ast_ctx* ctx);
+
+/* Launch geometry ast_fit_begin chose: threads per CTA, CTAs, register budget (CTAs of 256
+ * threads per SM the kernel was compiled for) and dynamic shared memory bytes.  Any pointer may
+ * be NULL.  No reference counterpart (the reference's geometry is the compile-time
+ * N_BLOCKS x BSIZE, asteroid.h:38-48). */
+int ast_fit_launch(ast_ctx* ctx, int32_t* tpb, int32_t* ctas, int32_t* min_ctas_per_sm, int32_t* smem_bytes);
 
 /* Device-side evaluation and fit counters since ast_fit_begin. */
 int ast_fit_counters(ast_ctx* ctx, int64_t* n_evals, int64_t* n_fits);
