@@ -331,3 +331,148 @@ def probe_peak(kind: str = "fp64", device: int = -1) -> float:
     g = C.c_double(0)
     check(lib.ast_probe_peak(int(device), 0 if kind == "fp64" else 1, C.byref(g)), "ast_probe_peak")
     return g.value
+
+
+def fit_cfg(n_chains=1024, group_size=256, seed=1, reopt=False, params0=None, precision=PREC_FP64, evals_cap=0,
+            steps_cap=0, n_stages=1, tpb=0):
+    """An ast_fit_cfg; the returned tuple keeps params0 alive while the struct is in use."""
+    cfg = capi.FitCfg()
+    cfg.seed = int(seed) & ((1 << 64) - 1)
+    cfg.n_chains = int(n_chains)
+    cfg.group_size = int(group_size)
+    cfg.n_stages = int(n_stages)
+    cfg.reopt = int(bool(reopt))
+    cfg.precision = int(precision)
+    cfg.evals_cap = int(evals_cap)
+    cfg.steps_cap = int(steps_cap)
+    cfg.tpb = int(tpb)
+    keep = None
+    if reopt:
+        keep = np.ascontiguousarray(params0, dtype=np.float64)
+        cfg.params0 = dptr(keep)
+    return cfg, keep
+
+
+def _result(n_chains, group_size, n_params, n_filters):
+    """An empty FitResult for one object and the ast_fit_out that points into it."""
+    G = n_chains // group_size
+    res = FitResult(np.zeros(G), np.zeros((G, n_params)), np.zeros((G, n_filters)), np.zeros(0), 0, n_chains, 0.0)
+    out = capi.FitOut()
+    out.best_f = dptr(res.best_f)
+    out.best_params = dptr(res.best_params)
+    out.best_dv = dptr(res.best_dv)
+    return res, out
+
+
+class Batch:
+    """Many objects fitted by one persistent, graph-captured launch (ast_batch_*)."""
+
+    def __init__(self, precision=PREC_MIXED, acc=True, n_slots=0, device=-1):
+        self.lib = capi.load()
+        h = C.c_void_p()
+        check(self.lib.ast_batch_create(int(device), int(precision), int(bool(acc)), int(n_slots), C.byref(h)),
+              "ast_batch_create")
+        self.h = h
+        self.precision = precision
+        self.items = []
+
+    def add(self, model, obs: Obs, **cfg_kw) -> int:
+        cfg, keep = fit_cfg(precision=self.precision, **cfg_kw)
+        idx = C.c_int32(-1)
+        cobs = obs.as_c()
+        check(self.lib.ast_batch_add(self.h, C.byref(model), C.byref(cobs), C.byref(cfg), C.byref(idx)), "ast_batch_add")
+        self.items.append((cfg.n_chains, cfg.group_size, model.n_params, obs.n_filters))
+        return idx.value
+
+    def tune(self, evals_per_slot=4) -> dict:
+        t = capi.BatchTune()
+        check(self.lib.ast_batch_tune(self.h, int(evals_per_slot), C.byref(t)), "ast_batch_tune")
+        return dict(tpb=t.tpb, refill=t.refill, ctas=t.ctas, evals_per_s=t.evals_per_s)
+
+    def run(self, tpb=0, refill=0) -> float:
+        ms = C.c_double(0)
+        t = None
+        if tpb:
+            t = capi.BatchTune()
+            t.tpb, t.refill = int(tpb), int(refill or 1)
+        check(self.lib.ast_batch_run(self.h, C.byref(t) if t is not None else None, C.byref(ms)), "ast_batch_run")
+        return ms.value
+
+    def result(self, index) -> FitResult:
+        n_chains, group, n_params, n_filters = self.items[index]
+        res, out = _result(n_chains, group, n_params, n_filters)
+        check(self.lib.ast_batch_result(self.h, int(index), C.byref(out)), "ast_batch_result")
+        return res
+
+    def counters(self) -> dict:
+        ne, nf = C.c_int64(0), C.c_int64(0)
+        tpb, refill, ctas = C.c_int32(0), C.c_int32(0), C.c_int32(0)
+        check(self.lib.ast_batch_counters(self.h, C.byref(ne), C.byref(nf), C.byref(tpb), C.byref(refill),
+                                          C.byref(ctas)), "ast_batch_counters")
+        return dict(n_evals=ne.value, n_fits=nf.value, tpb=tpb.value, refill=refill.value, ctas=ctas.value)
+
+    def close(self):
+        if self.h:
+            self.lib.ast_batch_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+class Server:
+    """Continuous batching of fit requests (ast_server_*, ast_submit, ast_poll)."""
+
+    def __init__(self, precision=PREC_MIXED, acc=True, n_slots=0, hbm_budget=0, device=-1):
+        self.lib = capi.load()
+        h = C.c_void_p()
+        check(self.lib.ast_server_create(int(device), int(precision), int(bool(acc)), int(n_slots), int(hbm_budget),
+                                         C.byref(h)), "ast_server_create")
+        self.h = h
+        self.precision = precision
+        self.items = {}
+
+    def submit(self, model, obs: Obs, **cfg_kw) -> int:
+        cfg, keep = fit_cfg(precision=self.precision, **cfg_kw)
+        rid = C.c_int64(-1)
+        cobs = obs.as_c()
+        check(self.lib.ast_submit(self.h, C.byref(model), C.byref(cobs), C.byref(cfg), C.byref(rid)), "ast_submit")
+        self.items[rid.value] = (cfg.n_chains, cfg.group_size, model.n_params, obs.n_filters)
+        return rid.value
+
+    def step(self, evals_per_slot=16):
+        r, q = C.c_int32(0), C.c_int32(0)
+        check(self.lib.ast_server_step(self.h, int(evals_per_slot), C.byref(r), C.byref(q)), "ast_server_step")
+        return r.value, q.value
+
+    def poll(self, request):
+        """(FitResult, latency seconds) once done, else None."""
+        n_chains, group, n_params, n_filters = self.items[request]
+        res, out = _result(n_chains, group, n_params, n_filters)
+        lat = C.c_double(0)
+        rc = check(self.lib.ast_poll(self.h, int(request), C.byref(out), C.byref(lat)), "ast_poll")
+        return (res, lat.value) if rc == 1 else None
+
+    def request_bytes(self, request) -> int:
+        return int(self.lib.ast_request_bytes(self.h, int(request)))
+
+    def stats(self) -> dict:
+        ne, used, budget = C.c_int64(0), C.c_int64(0), C.c_int64(0)
+        ms = C.c_double(0)
+        check(self.lib.ast_server_stats(self.h, C.byref(ne), C.byref(ms), C.byref(used), C.byref(budget)),
+              "ast_server_stats")
+        return dict(n_evals=ne.value, kernel_ms=ms.value, hbm_used=used.value, hbm_budget=budget.value)
+
+    def close(self):
+        if self.h:
+            self.lib.ast_server_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

@@ -112,6 +112,15 @@ class FitOut(C.Structure):
     ]
 
 
+class BatchTune(C.Structure):
+    _fields_ = [
+        ("tpb", C.c_int32),
+        ("refill", C.c_int32),
+        ("ctas", C.c_int32),
+        ("evals_per_s", C.c_double),
+    ]
+
+
 # Every function the header declares, with its ctypes signature.
 _P = C.c_void_p
 SIGNATURES = {
@@ -150,6 +159,22 @@ SIGNATURES = {
     "ast_stream": (C.c_void_p, [_P]),
     "ast_probe_peak": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_double)]),
     "ast_version": (C.c_char_p, []),
+    "ast_batch_create": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int64, C.POINTER(_P)]),
+    "ast_batch_add": (C.c_int, [_P, C.POINTER(Model), C.POINTER(ObsSet), C.POINTER(FitCfg), C.POINTER(C.c_int32)]),
+    "ast_batch_tune": (C.c_int, [_P, C.c_int64, C.POINTER(BatchTune)]),
+    "ast_batch_run": (C.c_int, [_P, C.POINTER(BatchTune), C.POINTER(C.c_double)]),
+    "ast_batch_result": (C.c_int, [_P, C.c_int32, C.POINTER(FitOut)]),
+    "ast_batch_counters": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int32),
+                                     C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "ast_batch_destroy": (None, [_P]),
+    "ast_server_create": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int64, C.c_int64, C.POINTER(_P)]),
+    "ast_submit": (C.c_int, [_P, C.POINTER(Model), C.POINTER(ObsSet), C.POINTER(FitCfg), C.POINTER(C.c_int64)]),
+    "ast_server_step": (C.c_int, [_P, C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "ast_poll": (C.c_int, [_P, C.c_int64, C.POINTER(FitOut), C.POINTER(C.c_double)]),
+    "ast_server_stats": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_double), C.POINTER(C.c_int64),
+                                   C.POINTER(C.c_int64)]),
+    "ast_request_bytes": (C.c_int64, [_P, C.c_int64]),
+    "ast_server_destroy": (None, [_P]),
 }
 
 _LIB = None

@@ -80,6 +80,38 @@ __global__ void prep_sums_kernel(DevModel M, char* base, ObsLayout L, int64_t n)
     if (blockIdx.x == 0 && threadIdx.x == 0) prep_obs_sums(M, base, L, n);
 }
 
+// Host image of an object's SoA block: t, V, w, filter and (without INTERP) the unit E and S
+// vectors; h, nst, the INTERP vectors and the mixed-path arrays are filled on the device.
+void obs_image(const ast_model* model, const ast_obs_set* obs, const ObsLayout& L, std::vector<unsigned char>& img)
+{
+    const int64_t n = obs->n_data;
+    img.assign((size_t)L.bytes, 0);
+    unsigned char* b = img.data();
+    memcpy(b + L.off_t, obs->mjd, 8 * n);
+    memcpy(b + L.off_v, obs->v, 4 * n);
+    memcpy(b + L.off_w, obs->w, 4 * n);
+    memcpy(b + L.off_f, obs->filter, 4 * n);
+    if (!(model->flags & AST_INTERP)) {
+        double* ex = (double*)(b + L.off_e);
+        double* sx = (double*)(b + L.off_s);
+        for (int64_t i = 0; i < n; i++)
+            for (int k = 0; k < 3; k++) {
+                ex[k * n + i] = obs->e_unit[3 * i + k];
+                sx[k * n + i] = obs->s_unit[3 * i + k];
+            }
+    }
+}
+
+// The parameter-independent preparation of an uploaded block (prep.cuh), stream-ordered.
+int launch_prep(const DevModel& dm, char* d_block, const ObsLayout& L, int64_t n, cudaStream_t s)
+{
+    prep_obs_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(dm, d_block, L, n);
+    AST_CUDA(cudaGetLastError());
+    prep_sums_kernel<<<1, 32, 0, s>>>(dm, d_block, L, n);
+    AST_CUDA(cudaGetLastError());
+    return AST_OK;
+}
+
 // One thread per parameter vector; the block's observations are staged into shared memory.
 template <class CF, int PREC>
 __global__ void __launch_bounds__(128) eval_kernel(DevModel M, const void* g_obs, ObsLayout L, int use_smem,
@@ -205,32 +237,15 @@ extern "C" int ast_prepare(const ast_model* model, const ast_obs_set* obs, int32
     c->n_filters = obs->n_filters;
     const int64_t n = obs->n_data;
     c->layout = ObsLayout::make(n);
-    // Host image of the SoA block; h, nst (and E, S under INTERP) are filled on the device.
-    std::vector<unsigned char> img((size_t)c->layout.bytes, 0);
-    unsigned char* b = img.data();
-    memcpy(b + c->layout.off_t, obs->mjd, 8 * n);
-    memcpy(b + c->layout.off_v, obs->v, 4 * n);
-    memcpy(b + c->layout.off_w, obs->w, 4 * n);
-    memcpy(b + c->layout.off_f, obs->filter, 4 * n);
-    if (!(model->flags & AST_INTERP)) {
-        double* ex = (double*)(b + c->layout.off_e);
-        double* sx = (double*)(b + c->layout.off_s);
-        for (int64_t i = 0; i < n; i++)
-            for (int k = 0; k < 3; k++) {
-                ex[k * n + i] = obs->e_unit[3 * i + k];
-                sx[k * n + i] = obs->s_unit[3 * i + k];
-            }
-    }
+    std::vector<unsigned char> img;
+    obs_image(model, obs, c->layout, img);
     if (cudaMalloc(&c->d_obs, (size_t)c->layout.bytes) != cudaSuccess) {
         cudaGetLastError();
         ast_destroy(c);
         return ast_set_error(AST_E_NOMEM, "ast_prepare: cudaMalloc(%lld) failed", (long long)c->layout.bytes);
     }
     AST_CUDA(cudaMemcpyAsync(c->d_obs, img.data(), (size_t)c->layout.bytes, cudaMemcpyHostToDevice, c->stream));
-    prep_obs_kernel<<<(unsigned)((n + 127) / 128), 128, 0, c->stream>>>(c->dm, (char*)c->d_obs, c->layout, n);
-    AST_CUDA(cudaGetLastError());
-    prep_sums_kernel<<<1, 32, 0, c->stream>>>(c->dm, (char*)c->d_obs, c->layout, n);
-    AST_CUDA(cudaGetLastError());
+    if ((rc = launch_prep(c->dm, (char*)c->d_obs, c->layout, n, c->stream))) { ast_destroy(c); return rc; }
     AST_CUDA(cudaStreamSynchronize(c->stream));
     *out = c;
     return AST_OK;

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <vector>
 #include "asteroid_gb300.h"
 #include "model.cuh"
 
@@ -85,4 +86,6 @@ struct ast_ctx {
 namespace ast {
 int build_dev_model(const ast_model* m, const ast_obs_set* obs, DevModel* dm);
 int set_device(int device);
+void obs_image(const ast_model* model, const ast_obs_set* obs, const ObsLayout& L, std::vector<unsigned char>& img);
+int launch_prep(const DevModel& dm, char* d_block, const ObsLayout& L, int64_t n, cudaStream_t s);
 }  // namespace ast

@@ -233,3 +233,27 @@ def generate(cfg: SynthConfig | str, outdir, vmod_fn=None) -> Synth:
              "dv_true": (dv + cfg.base_mag).tolist(), "param_names": api.param_names(model)}
     (out / "truth.json").write_text(json.dumps(truth, indent=1))
     return Synth(cfg, out, model, obs, x_true, p_true, dv + cfg.base_mag, files)
+
+
+# Variants of the batched workload (config 3), drawn evenly: LS + TORQUE, BC, BW_BALL, all with
+# ACC so that one batch (one simplex precision) holds them.
+BATCH_VARIANTS = ("TORQUE,ACC", "BC,ACC", "BW_BALL,ACC")
+
+
+def batch_config(i: int, seed: int = 1003) -> SynthConfig:
+    """Object i of the batched workload: log-uniform 50-2000 points, 1-4 filters, a span of
+    3-60 days in nightly 6 h windows, the variant BATCH_VARIANTS[i % 3]."""
+    rng = np.random.default_rng([seed, i])
+    n_points = int(round(np.exp(rng.uniform(np.log(50.0), np.log(2000.0)))))
+    n_filters = int(rng.integers(1, 5))
+    span = int(rng.integers(3, 61))
+    n_nights = span if span <= 10 else int(rng.integers(max(3, span // 4), span + 1))
+    chars = "RVBI"[:n_filters]
+    return SynthConfig(f"c3_{i}", BATCH_VARIANTS[i % 3], 1e-2, n_points, n_filters, span, n_nights, seed=seed * 100003 + i,
+                       filter_chars=chars, dv_range=0.5 if n_filters > 1 else 0.0)
+
+
+def generate_batch(n_objects: int, outdir, seed: int = 1003, vmod_fn=None) -> list:
+    """n_objects objects of the batched workload under outdir/<i>."""
+    out = Path(outdir)
+    return [generate(batch_config(i, seed), out / f"{i:04d}", vmod_fn) for i in range(n_objects)]

@@ -291,6 +291,65 @@ void* ast_stream(ast_ctx* ctx);
  * returns GFLOP/s in *gflops.  Used as the roofline denominator for CUDA-core bound kernels. */
 int ast_probe_peak(int32_t device, int32_t kind, double* gflops);
 
+/* ---------------------------------------------------------------- batched fits
+ * Many objects -- each with its own model variant, light curve, filter and parameter counts,
+ * seed and caps -- fitted by one persistent launch over a shared pool of chain slots, captured
+ * once as a CUDA graph and replayed by ast_batch_run.  No reference counterpart: the reference
+ * fits one object per process (asteroid.c:main).  Each object's results are those ast_fit gives
+ * for the same model, observations and configuration (one stage: cfg->n_stages must be 1).  All
+ * objects of a batch share the precision and the ACC flag given at creation. */
+typedef struct ast_batch ast_batch;
+
+typedef struct ast_batch_launch {
+    int32_t tpb;          /* threads per CTA (32..256, multiple of 32) */
+    int32_t refill;       /* 1: a slot takes a new chain as soon as its own finishes (thread per
+                             chain); 32: a warp takes 32 chains of one object at once (warp per
+                             object, no divergence between light curves) */
+    int32_t ctas;         /* CTAs of the launch (output) */
+    double evals_per_s;   /* rate measured by ast_batch_tune (output) */
+} ast_batch_launch;
+
+/* n_slots: persistent chain slots (0 = 256 per SM). */
+int ast_batch_create(int32_t device, int32_t precision, int32_t acc, int64_t n_slots, ast_batch** out);
+/* Upload one object; *index numbers objects from 0 in the order added. */
+int ast_batch_add(ast_batch* batch, const ast_model* model, const ast_obs_set* obs, const ast_fit_cfg* cfg,
+                  int32_t* index);
+/* Autotuner: times every (tpb, refill) candidate on this batch with bounded launches of
+ * evals_per_slot evaluations per slot, keeps the fastest for ast_batch_run and returns it. */
+int ast_batch_tune(ast_batch* batch, int64_t evals_per_slot, ast_batch_launch* best);
+/* Run every chain of every object to completion (tune NULL: the tuned or default geometry). */
+int ast_batch_run(ast_batch* batch, const ast_batch_launch* tune, double* kernel_ms);
+/* Results of object index, laid out as ast_fit_out of ast_fit (n_evals not filled). */
+int ast_batch_result(ast_batch* batch, int32_t index, ast_fit_out* out);
+int ast_batch_counters(ast_batch* batch, int64_t* n_evals, int64_t* n_fits, int32_t* tpb, int32_t* refill,
+                       int32_t* ctas);
+void ast_batch_destroy(ast_batch* batch);
+
+/* ---------------------------------------------------------------- serving
+ * Continuous batching of fit requests: ast_submit queues a request (an object and its fit
+ * configuration, n_stages = 1); each ast_server_step admits queued requests in arrival order
+ * while their device footprint (observations, start points, chain and group results) fits the
+ * HBM budget, runs the shared slot pool for evals_per_slot evaluations per slot, and retires the
+ * requests whose chains have all finished (results to the host, memory freed).  A request's
+ * chains start as soon as the chains submitted before it are taken, while those still run;
+ * its result does not depend on what else is in flight.  No reference counterpart. */
+typedef struct ast_server ast_server;
+
+/* hbm_budget_bytes <= 0: 150 GiB. */
+int ast_server_create(int32_t device, int32_t precision, int32_t acc, int64_t n_slots, int64_t hbm_budget_bytes,
+                      ast_server** out);
+int ast_submit(ast_server* server, const ast_model* model, const ast_obs_set* obs, const ast_fit_cfg* cfg,
+               int64_t* request);
+int ast_server_step(ast_server* server, int64_t evals_per_slot, int32_t* n_running, int32_t* n_queued);
+/* 1 and the result (and the seconds from ast_submit to retirement) once the request is done,
+ * 0 while it is queued or running, < 0 on error. */
+int ast_poll(ast_server* server, int64_t request, ast_fit_out* out, double* latency_s);
+int ast_server_stats(ast_server* server, int64_t* n_evals, double* kernel_ms, int64_t* hbm_used,
+                     int64_t* hbm_budget);
+/* Device bytes the request holds while admitted (what admission counts against the budget). */
+int64_t ast_request_bytes(ast_server* server, int64_t request);
+void ast_server_destroy(ast_server* server);
+
 /* Library version string. */
 const char* ast_version(void);
 

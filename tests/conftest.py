@@ -63,13 +63,15 @@ _SYNTH_CACHE: dict = {}
 
 @pytest.fixture(scope="session")
 def synth_objects(built, oracle_mod, tmp_path_factory):
-    """Synthetic objects of the benchmark configurations, with oracle true-model curves."""
+    """Synthetic objects of the benchmark configurations ("c0" ... "c2", or "c3_<i>" for object i
+    of the batched workload), with oracle true-model curves."""
     from asteroid_gb300 import synth
 
     def get(name: str):
         if name not in _SYNTH_CACHE:
             d = tmp_path_factory.mktemp(f"synth_{name}")
-            _SYNTH_CACHE[name] = synth.generate(name, d, vmod_fn=lambda m, o, p: oracle_mod.model_curve(m, o, p))
+            cfg = synth.batch_config(int(name[3:])) if name.startswith("c3_") else name
+            _SYNTH_CACHE[name] = synth.generate(cfg, d, vmod_fn=lambda m, o, p: oracle_mod.model_curve(m, o, p))
         return _SYNTH_CACHE[name]
 
     return get

@@ -1,0 +1,119 @@
+"""Batched fits (ast_batch_*) and served fits (ast_server_*, ast_submit, ast_poll).
+
+Every object of a batch, and every request of a server, must come out exactly as a
+single-object ast_fit with the same model, observations and configuration: the chain's random
+draws are keyed by the object's seed and the chain's index within the object, and the
+evaluation is the same code, so neither the other objects in flight, nor the slot a chain runs
+on, nor the refill mapping may change a result.
+"""
+import numpy as np
+import pytest
+
+from asteroid_gb300 import api
+
+pytestmark = pytest.mark.gpu
+
+OBJECTS = ["c3_0", "c3_1", "c3_2", "c3_3", "c0acc"]
+CFG = dict(n_chains=256, group_size=64, seed=7, evals_cap=40)
+
+
+def single(s, precision, seed):
+    with api.Engine(s.model, s.obs) as eng:
+        return eng.fit(n_chains=CFG["n_chains"], group_size=CFG["group_size"], n_stages=1, seed=seed,
+                       evals_cap=CFG["evals_cap"], precision=precision)
+
+
+def same(a, b):
+    assert np.array_equal(a.best_f, b.best_f), (a.best_f, b.best_f)
+    assert np.array_equal(a.best_params, b.best_params)
+    assert np.array_equal(a.best_dv, b.best_dv)
+
+
+@pytest.mark.parametrize("precision", [api.PREC_FP64, api.PREC_MIXED])
+def test_batch_objects_equal_single_fits(gpu, synth_objects, precision):
+    objs = [synth_objects(n) for n in OBJECTS]
+    with api.Batch(precision=precision, acc=True, n_slots=152 * 64) as b:
+        idx = [b.add(s.model, s.obs, **dict(CFG, seed=CFG["seed"] + k)) for k, s in enumerate(objs)]
+        b.run()
+        got = [b.result(i) for i in idx]
+        c = b.counters()
+        assert c["n_fits"] == len(objs) * CFG["n_chains"]
+    for k, s in enumerate(objs):
+        same(got[k], single(s, precision, CFG["seed"] + k))
+
+
+def test_batch_refill_and_geometry_do_not_change_results(gpu, synth_objects):
+    objs = [synth_objects(n) for n in OBJECTS[:4]]
+    res = []
+    for tpb, refill in ((256, 1), (64, 32), (128, 32)):
+        with api.Batch(precision=api.PREC_MIXED, acc=True, n_slots=152 * 32) as b:
+            for k, s in enumerate(objs):
+                b.add(s.model, s.obs, **dict(CFG, seed=3 + k))
+            b.run(tpb=tpb, refill=refill)
+            assert b.counters()["refill"] == refill
+            res.append([b.result(i) for i in range(len(objs))])
+    for r in res[1:]:
+        for a, b_ in zip(res[0], r):
+            same(a, b_)
+
+
+def test_batch_tuner_picks_a_measured_candidate(gpu, synth_objects):
+    objs = [synth_objects(n) for n in OBJECTS[:3]]
+    with api.Batch(precision=api.PREC_MIXED, acc=True) as b:
+        for k, s in enumerate(objs):
+            b.add(s.model, s.obs, **dict(CFG, seed=11 + k))
+        t = b.tune(evals_per_slot=2)
+        assert t["tpb"] in (64, 128, 256) and t["refill"] in (1, 32) and t["evals_per_s"] > 0
+        b.run()
+        assert all(np.all(np.isfinite(b.result(i).best_f)) for i in range(3))
+
+
+def test_server_request_alone_equals_request_in_mix(gpu, synth_objects):
+    a, others = synth_objects("c3_3"), [synth_objects(n) for n in ("c3_0", "c3_1", "c3_2")]
+    cfg_a = dict(CFG, seed=99)
+    with api.Server(precision=api.PREC_MIXED, acc=True, n_slots=152 * 64) as srv:
+        r = srv.submit(a.model, a.obs, **cfg_a)
+        while srv.poll(r) is None:
+            srv.step(8)
+        alone, _ = srv.poll(r)
+    with api.Server(precision=api.PREC_MIXED, acc=True, n_slots=152 * 64) as srv:
+        ids = [srv.submit(s.model, s.obs, **dict(CFG, seed=20 + k)) for k, s in enumerate(others)]
+        srv.step(4)
+        srv.step(4)
+        r = srv.submit(a.model, a.obs, **cfg_a)  # arrives while the others run
+        while any(srv.poll(i) is None for i in ids + [r]):
+            srv.step(8)
+        mixed, lat = srv.poll(r)
+        assert lat > 0
+        in_mix_others = [srv.poll(i)[0] for i in ids]
+    same(alone, mixed)
+    same(alone, single(a, api.PREC_MIXED, 99))
+    for k, s in enumerate(others):
+        with api.Engine(s.model, s.obs) as eng:
+            ref = eng.fit(n_chains=CFG["n_chains"], group_size=CFG["group_size"], seed=20 + k,
+                          evals_cap=CFG["evals_cap"], precision=api.PREC_MIXED)
+        same(in_mix_others[k], ref)
+
+
+def test_server_admits_by_hbm_budget(gpu, synth_objects):
+    s = synth_objects("c3_1")
+    with api.Server(precision=api.PREC_FP64, acc=True, n_slots=152 * 32, hbm_budget=1) as srv:
+        with pytest.raises(api.capi.AstError):
+            srv.submit(s.model, s.obs, **CFG)  # larger than the whole budget
+    # Three requests of the same footprint; the budget holds one and a half: one runs at a time
+    # and the others wait in arrival order.
+    with api.Server(precision=api.PREC_FP64, acc=True, n_slots=152 * 32, hbm_budget=1 << 40) as probe:
+        need = probe.request_bytes(probe.submit(s.model, s.obs, **CFG))
+    budget = need + need // 2
+    with api.Server(precision=api.PREC_FP64, acc=True, n_slots=152 * 32, hbm_budget=budget) as srv:
+        ids = [srv.submit(s.model, s.obs, **dict(CFG, seed=5 + k)) for k in range(3)]
+        running, queued = srv.step(4)
+        assert running == 1 and queued == 2
+        peak = 0
+        while any(srv.poll(i) is None for i in ids):
+            running, queued = srv.step(16)
+            st = srv.stats()
+            peak = max(peak, st["hbm_used"])
+            assert st["hbm_used"] <= st["hbm_budget"] and running <= 1
+        for k, i in enumerate(ids):
+            same(srv.poll(i)[0], single(s, api.PREC_FP64, 5 + k))
