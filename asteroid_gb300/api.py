@@ -255,6 +255,13 @@ class Engine:
         check(self.lib.ast_model_curve(self.ctx, dptr(p), dptr(out)), "ast_model_curve")
         return out
 
+    def model_angles(self, params, precision: int = PREC_FP64) -> np.ndarray:
+        """Euler angles [n_data, 3] along the FP64 or the mixed-precision integration."""
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        out = np.zeros((self.obs.n_data, 3))
+        check(self.lib.ast_model_angles(self.ctx, int(precision), dptr(p), dptr(out)), "ast_model_angles")
+        return out
+
     def _cfg(self, n_chains, group_size, n_stages, seed, reopt, params0, precision, evals_cap, steps_cap, tpb,
              min_ctas_per_sm=0, stage_obs=0):
         cfg = capi.FitCfg()
@@ -397,6 +404,12 @@ class Batch:
             t.tpb, t.refill = int(tpb), int(refill or 1)
         check(self.lib.ast_batch_run(self.h, C.byref(t) if t is not None else None, C.byref(ms)), "ast_batch_run")
         return ms.value
+
+    def step(self, evals_per_slot: int) -> tuple:
+        """One bounded launch: (done, kernel ms)."""
+        done, ms = C.c_int32(0), C.c_double(0)
+        check(self.lib.ast_batch_step(self.h, int(evals_per_slot), C.byref(done), C.byref(ms)), "ast_batch_step")
+        return bool(done.value), ms.value
 
     def result(self, index) -> FitResult:
         n_chains, group, n_params, n_filters = self.items[index]

@@ -132,6 +132,7 @@ SIGNATURES = {
     "ast_x2params": (C.c_int, [C.POINTER(Model), C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "ast_params2x": (C.c_int, [C.POINTER(Model), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "ast_model_curve": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "ast_model_angles": (C.c_int, [_P, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "ast_read_data": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int32, C.c_int32, C.POINTER(C.POINTER(HostData))]),
     "ast_read_minima": (C.c_int, [C.c_char_p, C.POINTER(HostData)]),
     "ast_free_host_data": (None, [C.POINTER(HostData)]),
@@ -163,6 +164,7 @@ SIGNATURES = {
     "ast_batch_add": (C.c_int, [_P, C.POINTER(Model), C.POINTER(ObsSet), C.POINTER(FitCfg), C.POINTER(C.c_int32)]),
     "ast_batch_tune": (C.c_int, [_P, C.c_int64, C.POINTER(BatchTune)]),
     "ast_batch_run": (C.c_int, [_P, C.POINTER(BatchTune), C.POINTER(C.c_double)]),
+    "ast_batch_step": (C.c_int, [_P, C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
     "ast_batch_result": (C.c_int, [_P, C.c_int32, C.POINTER(FitOut)]),
     "ast_batch_counters": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int32),
                                      C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),

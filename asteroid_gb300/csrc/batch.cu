@@ -685,9 +685,57 @@ static int batch_tune_t(ast_batch* B, int64_t evals_per_slot, ast_batch_launch* 
         }
     int rc = pool_geometry<CF, PREC>(B->P, bt.tpb, bt.refill);
     if (rc) return rc;
+    // Back to the untouched state: the probes ran chains that the batch will run again.
+    ast_pool& P = B->P;
+    batch_reset_kernel<<<(unsigned)((P.S + 255) / 256), 256, 0, P.stream>>>(P.chain, P.st, P.it, P.ev, P.S);
+    AST_CUDA(cudaMemsetAsync(P.ctr, 0, 64, P.stream));
+    AST_CUDA(cudaMemsetAsync(P.done, 0, (size_t)P.cap * 8, P.stream));
+    AST_CUDA(cudaStreamSynchronize(P.stream));
     bt.ctas = B->P.ctas;
     bt.evals_per_s = best_rate;
     if (best) *best = bt;
+    return AST_OK;
+}
+
+// One bounded launch from the batch's current state (no graph): every slot performs at most
+// evals_per_slot evaluations; when the last chain has finished, the group argmins run and the
+// results come back.
+template <class CF, int PREC>
+static int batch_step_t(ast_batch* B, int64_t evals_per_slot, int32_t* done, double* kernel_ms)
+{
+    ast_pool& P = B->P;
+    int rc;
+    if (!P.ctas && (rc = pool_geometry<CF, PREC>(P, 256, 1))) return rc;
+    if ((rc = upload_table<CF>(P))) return rc;
+    const FitView<CF> V = pool_view<CF>(P);
+    AST_CUDA(cudaEventRecord(P.ev0, P.stream));
+    batch_kernel_ptr<CF, PREC>(P.refill)<<<P.ctas, P.tpb, 0, P.stream>>>((const BatchObj<CF>*)P.d_objs,
+                                                                           (int)P.active.size(), V, evals_per_slot);
+    AST_CUDA(cudaGetLastError());
+    AST_CUDA(cudaEventRecord(P.ev1, P.stream));
+    unsigned long long h[8];
+    AST_CUDA(cudaMemcpyAsync(h, P.ctr, sizeof(h), cudaMemcpyDeviceToHost, P.stream));
+    AST_CUDA(cudaStreamSynchronize(P.stream));
+    float ms = 0;
+    AST_CUDA(cudaEventElapsedTime(&ms, P.ev0, P.ev1));
+    P.kernel_ms += ms;
+    P.evals = h[2];
+    P.fits = h[3];
+    if (kernel_ms) *kernel_ms = ms;
+    *done = h[1] >= (unsigned long long)P.chain_end;
+    if (*done) {
+        std::vector<std::pair<int, Entry*>> all;
+        for (size_t k = 0; k < P.active.size(); k++) all.push_back({(int)k, P.active[k]});
+        int n_blocks = 0;
+        if ((rc = fill_gmap(P, all, &n_blocks))) return rc;
+        batch_group_best_kernel<CF><<<(unsigned)n_blocks, 256, 0, P.stream>>>((const BatchObj<CF>*)P.d_objs, P.d_gmap, V);
+        AST_CUDA(cudaGetLastError());
+        for (Entry* e : P.active) {
+            if ((rc = fetch_results(P, e))) return rc;
+            e->state = 2;
+        }
+        B->ran = true;
+    }
     return AST_OK;
 }
 
@@ -726,6 +774,7 @@ extern "C" int ast_batch_add(ast_batch* B, const ast_model* model, const ast_obs
 extern "C" int ast_batch_tune(ast_batch* B, int64_t evals_per_slot, ast_batch_launch* best)
 {
     if (!B || B->P.active.empty()) return ast_set_error(AST_E_INVALID, "ast_batch_tune: empty batch");
+    if (B->ran) return ast_set_error(AST_E_INVALID, "ast_batch_tune: the batch has finished");
     int rc = set_device(B->P.device);
     if (rc) return rc;
     if (evals_per_slot <= 0) evals_per_slot = 4;
@@ -738,6 +787,16 @@ extern "C" int ast_batch_run(ast_batch* B, const ast_batch_launch* tune, double*
     int rc = set_device(B->P.device);
     if (rc) return rc;
     return AST_DISPATCH(B->P, batch_run_t, B, tune, kernel_ms);
+}
+
+extern "C" int ast_batch_step(ast_batch* B, int64_t evals_per_slot, int32_t* done, double* kernel_ms)
+{
+    if (!B || !done || B->P.active.empty()) return ast_set_error(AST_E_INVALID, "ast_batch_step: bad argument");
+    if (B->ran) return ast_set_error(AST_E_INVALID, "ast_batch_step: the batch has finished");
+    int rc = set_device(B->P.device);
+    if (rc) return rc;
+    if (evals_per_slot <= 0) evals_per_slot = INT64_MAX;
+    return AST_DISPATCH(B->P, batch_step_t, B, evals_per_slot, done, kernel_ms);
 }
 
 extern "C" int ast_batch_result(ast_batch* B, int32_t index, ast_fit_out* out)

@@ -160,6 +160,24 @@ __global__ void model_curve_kernel(DevModel M, const void* g_obs, ObsLayout L, c
     chi2_fp64<double>(M2, o, p, d, vmod);
 }
 
+// Euler angles at every observation along the FP64 or the mixed-precision integration.
+template <int PREC>
+__global__ void model_angles_kernel(DevModel M, const void* g_obs, ObsLayout L, const double* params, double* ang)
+{
+    __shared__ float4 trig[kTrigTable];
+    trig_table_fill(trig);
+    __syncthreads();
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    const ObsView o = L.view(g_obs, M.n_data);
+    double p[AST_MAX_PARAMS];
+    for (int i = 0; i < M.n_params; i++) p[i] = params[i];
+    double d[AST_MAX_FILTERS];
+    DevModel M2 = M;
+    M2.flags &= ~AST_NUDGE;
+    if (PREC == AST_PREC_FP64) chi2_fp64<double>(M2, o, p, d, nullptr, ang);
+    else chi2_mixed<double>(M2, o, p, d, trig, ang);
+}
+
 // FMA throughput probe (roofline denominators for CUDA-core bound kernels).
 template <class T>
 __global__ void fma_probe_kernel(T* out, int iters, T a, T b)
@@ -390,6 +408,33 @@ extern "C" int ast_model_curve(ast_ctx* c, const double* params, double* vmod)
     AST_CUDA(cudaStreamSynchronize(c->stream));
     cudaFree(dp);
     cudaFree(dv);
+    return AST_OK;
+}
+
+extern "C" int ast_model_angles(ast_ctx* c, int32_t precision, const double* params, double* angles)
+{
+    if (!c || !params || !angles) return ast_set_error(AST_E_INVALID, "ast_model_angles: NULL argument");
+    if (precision != AST_PREC_FP64 && precision != AST_PREC_MIXED)
+        return ast_set_error(AST_E_INVALID, "ast_model_angles: bad precision");
+    int rc = set_device(c->device);
+    if (rc) return rc;
+    double *dp = nullptr, *da = nullptr;
+    if (cudaMalloc(&dp, sizeof(double) * AST_MAX_PARAMS) != cudaSuccess ||
+        cudaMalloc(&da, sizeof(double) * 3 * c->n_data) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(dp);
+        return ast_set_error(AST_E_NOMEM, "ast_model_angles: cudaMalloc failed");
+    }
+    AST_CUDA(cudaMemcpyAsync(dp, params, sizeof(double) * c->model.n_params, cudaMemcpyHostToDevice, c->stream));
+    if (precision == AST_PREC_FP64)
+        model_angles_kernel<AST_PREC_FP64><<<1, 32, 0, c->stream>>>(c->dm, c->d_obs, c->layout, dp, da);
+    else
+        model_angles_kernel<AST_PREC_MIXED><<<1, 32, 0, c->stream>>>(c->dm, c->d_obs, c->layout, dp, da);
+    AST_CUDA(cudaGetLastError());
+    AST_CUDA(cudaMemcpyAsync(angles, da, sizeof(double) * 3 * c->n_data, cudaMemcpyDeviceToHost, c->stream));
+    AST_CUDA(cudaStreamSynchronize(c->stream));
+    cudaFree(dp);
+    cudaFree(da);
     return AST_OK;
 }
 

@@ -127,10 +127,19 @@ AST_HD double vmod_fp64(const DevModel& M, const ObsView& o, const double* param
 // the right-hand side small enough for the instruction cache).
 AST_HD void df_sincos2(df a0, df a1, const float4* tab, df* s0, df* c0, df* s1, df* c1)
 {
-    df sv[2], cv[2];
 #pragma unroll 1
-    for (int q = 0; q < 2; q++) df_sincos(q ? a1 : a0, tab, &sv[q], &cv[q]);
-    *s0 = sv[0]; *c0 = cv[0]; *s1 = sv[1]; *c1 = cv[1];
+    for (int q = 0; q < 2; q++) {
+        df s, c;
+        df_sincos(q ? a1 : a0, tab, &s, &c);
+        // Selects, not an array indexed by q: the results stay in registers.
+        if (q == 0) {
+            *s0 = s;
+            *c0 = c;
+        } else {
+            *s1 = s;
+            *c1 = c;
+        }
+    }
 }
 
 AST_HD void ode_torque_df(const df* y, df* f, const df* mu, const float4* tab)
@@ -343,9 +352,11 @@ static __host__ __device__ __noinline__ bool nudge_flush(const DevModel& M, cons
     return true;
 }
 
-// Same contract as chi2_fp64 (model.cuh); tab is the shared-memory sin/cos table.
+// Same contract as chi2_fp64 (model.cuh); tab is the shared-memory sin/cos table; ang_out, when
+// non-null, receives the Euler angles at every observation (reduced to [-pi, pi]).
 template <class CF>
-__host__ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const double* params, CF* delta_V, const float4* tab)
+__host__ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const double* params, CF* delta_V, const float4* tab,
+                                  double* ang_out = nullptr)
 {
     const int flags = M.flags;
     const ast_type_ids& T = M.t;
@@ -451,13 +462,29 @@ __host__ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const dou
         // The Euler angles enter the right-hand side and the brightness only through sin and
         // cos, so they are kept reduced to [-pi, pi]: the double-float then resolves the phase
         // to ~1e-14 rad instead of u^2 of the accumulated angle.
-        const int a0 = torque ? 3 : 0;
-#pragma unroll
-        for (int k = 0; k < 3; k++) y[a0 + k] = df_reduce_2pi(y[a0 + k]);
+        // (Constant indices only: an index computed at run time would move y to local memory.)
+        df ang[3];
+        if (torque) {
+            y[3] = df_reduce_2pi(y[3]);
+            y[4] = df_reduce_2pi(y[4]);
+            y[5] = df_reduce_2pi(y[5]);
+            ang[0] = y[3];
+            ang[1] = y[4];
+            ang[2] = y[5];
+        } else {
+            y[0] = df_reduce_2pi(y[0]);
+            y[1] = df_reduce_2pi(y[1]);
+            y[2] = df_reduce_2pi(y[2]);
+            ang[0] = y[0];
+            ang[1] = y[1];
+            ang[2] = y[2];
+        }
+        if (ang_out)
+            for (int k = 0; k < 3; k++) ang_out[3 * i + k] = df_to_double(ang[k]);
         float sin_phi, cos_phi, sin_theta, cos_theta, sin_psi, cos_psi;
-        sincosf(DF_ADD(y[a0].hi, y[a0].lo), &sin_phi, &cos_phi);
-        sincosf(DF_ADD(y[a0 + 1].hi, y[a0 + 1].lo), &sin_theta, &cos_theta);
-        sincosf(DF_ADD(y[a0 + 2].hi, y[a0 + 2].lo), &sin_psi, &cos_psi);
+        sincosf(DF_ADD(ang[0].hi, ang[0].lo), &sin_phi, &cos_phi);
+        sincosf(DF_ADD(ang[1].hi, ang[1].lo), &sin_theta, &cos_theta);
+        sincosf(DF_ADD(ang[2].hi, ang[2].lo), &sin_psi, &cos_psi);
         float N_x = XM_x * cos_phi + YM_x * sin_phi;
         float N_y = YM_y * sin_phi;
         float N_z = XM_z * cos_phi + YM_z * sin_phi;
@@ -515,7 +542,7 @@ __host__ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const dou
             // FP32 magnitude is used only to rule a triple out with a margin far above its error;
             // a candidate triple is queued with its double-float angles and re-evaluated with
             // double-float magnitudes (nudge_flush), in order, exactly as the reference tests it.
-            const df ang_i[3] = {torque ? y[3] : y[0], torque ? y[4] : y[1], torque ? y[5] : y[2]};
+            const df ang_i[3] = {ang[0], ang[1], ang[2]};
             if (i >= 2) {
                 bool local = false;
                 for (int ii = 0; ii < M.n_min; ii++)

@@ -349,10 +349,11 @@ struct Geometry {
 // Returns CHI_FLOAT; delta_V is written only when the evaluation runs to the end (the NUDGE
 // "more than M_MAX minima" exit returns 1e30 and leaves it, as the reference does).
 // vmod_out, when non-null, receives the model magnitude of every observation (the reference's
-// Nplot > 0 mode, cuda.c:699-704, without the delta_V shift).
+// Nplot > 0 mode, cuda.c:699-704, without the delta_V shift); ang_out the Euler angles
+// (phi, theta, psi) at every observation.
 template <class CF>
 __device__ CF chi2_fp64(const DevModel& M, const ObsView& o, const double* params, CF* delta_V,
-                        double* vmod_out = nullptr)
+                        double* vmod_out = nullptr, double* ang_out = nullptr)
 {
     const int flags = M.flags;
     const ast_type_ids& T = M.t;
@@ -436,6 +437,11 @@ __device__ CF chi2_fp64(const DevModel& M, const ObsView& o, const double* param
         const double phi = torque ? y[3] : y[0];
         const double theta = torque ? y[4] : y[1];
         const double psi = torque ? y[5] : y[2];
+        if (ang_out) {
+            ang_out[3 * i] = phi;
+            ang_out[3 * i + 1] = theta;
+            ang_out[3 * i + 2] = psi;
+        }
 
         double cos_phi, sin_phi;
         sincos(phi, &sin_phi, &cos_phi);

@@ -221,6 +221,151 @@ def run_fit_steps(eng, precision, n_chains, group, evals_cap, budget, warmup, st
     return e1 - e0, ms, f1 - f0, steps, budget
 
 
+def run_batch_steps(s, precision, n_chains, group, evals_cap, budget, warmup, steps, seed, stream_events, reopt,
+                    params0):
+    """Evaluations/s of bounded ast_batch_step launches with the workload as one batch object."""
+    from asteroid_gb300 import api
+
+    kw = dict(n_chains=n_chains, group_size=group, seed=seed, evals_cap=evals_cap)
+    if reopt:
+        kw.update(reopt=True, params0=params0)
+    with api.Batch(precision=precision, acc=bool(s.model.flags & api.ACC)) as b:
+        b.add(s.model, s.obs, **kw)
+        for _ in range(warmup):
+            b.step(budget)
+        e0 = b.counters()["n_evals"]
+        t = [0.0]
+
+        def go():
+            for _ in range(steps):
+                t[0] += b.step(budget)[1]
+
+        stream_events(go)
+        e1 = b.counters()["n_evals"]
+    return (e1 - e0) / (t[0] * 1e-3)
+
+
+def wrap(a):
+    return (a + np.pi) % (2 * np.pi) - np.pi
+
+
+def phase_drift(eng, model, obs, truth, vectors):
+    """Largest |mixed - FP64| Euler angle (rad, modulo 2 pi) over the light curve, for the true
+    model and a few workload vectors, and the total rotation phase the FP64 path accumulates."""
+    from asteroid_gb300 import api
+
+    out = {"max_rad": 0.0, "at_last_point_rad": 0.0, "total_phase_rad": 0.0,
+           "span_days": float(obs.mjd[-1] - obs.mjd[0]), "vectors": 0}
+    for p in np.vstack([truth, vectors]):
+        a64 = eng.model_angles(p, api.PREC_FP64)
+        a32 = eng.model_angles(p, api.PREC_MIXED)
+        if not (np.all(np.isfinite(a64)) and np.all(np.isfinite(a32))):
+            continue
+        d = np.abs(wrap(a32 - a64))
+        out["max_rad"] = max(out["max_rad"], float(d.max()))
+        out["at_last_point_rad"] = max(out["at_last_point_rad"], float(d[-1].max()))
+        out["total_phase_rad"] = max(out["total_phase_rad"], float(np.abs(a64[-1] - a64[0]).max()))
+        out["vectors"] += 1
+    return out
+
+
+def bench_batch(args, tmp, rank, world):
+    """Config 3: uneven objects (log-uniform 50-2000 points, 1-4 filters, 3-60 day spans, LS+TORQUE
+    / BC / BW_BALL) with 1024 chains each, as one batch: the autotuned geometry, then bounded
+    timed launches (evals/s), FP64 beside it, and one graph-captured run to completion of the
+    whole batch at a small evaluation cap."""
+    import torch
+
+    from asteroid_gb300 import api, synth
+
+    objs = synth.generate_batch(args.objects, tmp)
+    stream_events = lambda fn: (fn(), None)
+    line = {"metric": METRIC, "unit": UNIT, "mode": "batch", "objects": len(objs), "chains_per_object": 1024,
+            "data": "synthetic (config-3 generator)"}
+    for prec, name in ((api.PREC_MIXED, "mixed"), (api.PREC_FP64, "fp64")):
+        with api.Batch(precision=prec, acc=True) as b:
+            for k, s in enumerate(objs):
+                b.add(s.model, s.obs, n_chains=1024, group_size=256, seed=17 + k, evals_cap=5000)
+            tune = b.tune(evals_per_slot=2)
+            budget = 4 if prec == api.PREC_MIXED else 2
+            for _ in range(args.warmup):
+                b.step(budget)
+            e0 = b.counters()["n_evals"]
+            ms = 0.0
+            for _ in range(args.steps):
+                ms += b.step(budget)[1]
+            e1 = b.counters()["n_evals"]
+            line[name] = {"value": (e1 - e0) / (ms * 1e-3), "tuned": tune, "timed_evals": e1 - e0, "ms": ms}
+    line["speedup_mixed_over_fp64"] = line["mixed"]["value"] / line["fp64"]["value"]
+    # The whole batch in one graph-captured persistent launch (evaluation cap 50 per chain).
+    with api.Batch(precision=api.PREC_MIXED, acc=True) as b:
+        for k, s in enumerate(objs):
+            b.add(s.model, s.obs, n_chains=1024, group_size=256, seed=17 + k, evals_cap=50)
+        b.tune(evals_per_slot=2)
+        ms = b.run()
+        c = b.counters()
+        line["graph_run"] = {"evals_cap": 50, "ms": ms, "evals": c["n_evals"], "fits": c["n_fits"],
+                             "evals_per_s": c["n_evals"] / (ms * 1e-3), "geometry": c}
+    print(json.dumps(line))
+
+
+def bench_serve(args, tmp, rank, world):
+    """Config 4: Poisson arrivals of config-3 objects (1024 chains x 5000 evaluations each) at 1, 4,
+    16 and 64 requests/s into one server (150 GB HBM budget); p50/p99 latency from submission to
+    retirement, fits/s, and each served best chi^2 re-evaluated by the FP64 path."""
+    from asteroid_gb300 import api, synth
+
+    pool = synth.generate_batch(32, tmp)
+    rng = np.random.default_rng(2024)
+    line = {"metric": "fit_latency", "unit": "s", "mode": "serve", "requests_per_rate": args.requests,
+            "chains_per_request": 1024, "evals_per_chain": 5000, "hbm_budget_gb": 150, "rates": {}}
+    worst = 0.0
+    engines = {}
+    for lam in (1.0, 4.0, 16.0, 64.0):
+        arrivals = np.cumsum(rng.exponential(1.0 / lam, size=args.requests))
+        with api.Server(precision=api.PREC_MIXED, acc=True, hbm_budget=150 << 30) as srv:
+            t0 = time.perf_counter()
+            ids, objs, done, lat = [], [], {}, {}
+            k = 0
+            while len(done) < args.requests:
+                now = time.perf_counter() - t0
+                while k < args.requests and arrivals[k] <= now:
+                    s = pool[(k * 7 + int(lam)) % len(pool)]
+                    ids.append(srv.submit(s.model, s.obs, n_chains=1024, group_size=256, seed=100 + k, evals_cap=5000))
+                    objs.append(s)
+                    k += 1
+                if not ids or len(done) == len(ids):
+                    time.sleep(max(0.0, min(0.01, arrivals[k] - now)) if k < args.requests else 0.0)
+                    continue
+                srv.step(32)
+                for j, r in enumerate(ids):
+                    if r not in done:
+                        got = srv.poll(r)
+                        if got is not None:
+                            done[r] = got[0]
+                            lat[r] = got[1]
+            wall = time.perf_counter() - t0
+            st = srv.stats()
+        L = np.array([lat[r] for r in ids])
+        # Served results against FP64: the best group's parameters re-evaluated by the plain path.
+        for r, s in zip(ids, objs):
+            res = done[r]
+            g = res.best
+            key = id(s)
+            if key not in engines:
+                engines[key] = api.Engine(s.model, s.obs)
+            c64, _ = engines[key].eval(res.best_params[g][None, :], api.PREC_FP64)
+            if np.isfinite(c64[0]) and c64[0] < 1e29:
+                worst = max(worst, abs(res.best_f[g] - c64[0]) / abs(c64[0]))
+        line["rates"][f"{lam:g}/s"] = {"p50_s": float(np.percentile(L, 50)), "p99_s": float(np.percentile(L, 99)),
+                                       "fits_per_s": len(ids) / wall, "wall_s": wall,
+                                       "evals_per_s": st["n_evals"] / (st["kernel_ms"] * 1e-3)}
+    for e in engines.values():
+        e.close()
+    line["served_vs_fp64_max_rel_dchi2"] = worst
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -233,6 +378,12 @@ def main():
     ap.add_argument("--budget-mixed", type=int, default=0, help="evaluations per slot per step (0 = auto)")
     ap.add_argument("--budget-fp64", type=int, default=0)
     ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--skip-batched", action="store_true")
+    ap.add_argument("--mode", default="fit", choices=["fit", "batch", "serve"],
+                    help="fit: the headline line; batch: config 3 (uneven objects, one launch); "
+                         "serve: config 4 (Poisson arrivals, continuous batching)")
+    ap.add_argument("--objects", type=int, default=512, help="batch mode: objects")
+    ap.add_argument("--requests", type=int, default=8, help="serve mode: requests per arrival rate")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--profile", action="store_true", help="only the fit launches (for ncu)")
@@ -285,6 +436,10 @@ def main():
 
     build.build_engine()
     torch.cuda.set_device(local)
+    if args.mode == "batch":
+        return bench_batch(args, tmp, rank, world)
+    if args.mode == "serve":
+        return bench_serve(args, tmp, rank, world)
     s = make_workload(args, tmp)
     model, obs = s.model, s.obs
     eng = api.Engine(model, obs, device=local)
@@ -308,7 +463,9 @@ def main():
 
     n_rk4 = rk4_steps(obs, model.time_step)
     flops, trans = algorithmic_flops(obs, model)
-    seed = 1234 + 7919 * rank
+    from asteroid_gb300 import replicas
+
+    seed = replicas.replica_seed(1234, rank)  # one replica per GPU, distinct seeds
 
     # NUDGE is the reference's Stage-Three option, run with -reopt from a good model
     # (README.md:88-103): chains start around the true model.  From random starts nearly every
@@ -334,6 +491,10 @@ def main():
     ev_m_all = sum_over_ranks(dist, ev_m)
     value = ev_m_all / (ms_m * 1e-3)
 
+    # The same workload through the batch engine (ast_batch_step): one object of the batch path.
+    batched = run_batch_steps(s, api.PREC_MIXED, args.chains, 256, args.evals_cap, b_mixed, args.warmup, args.steps,
+                              seed, timed, reopt, p0) if not args.skip_batched else None
+
     fp64 = None
     if not args.skip_fp64:
         ev_d, ms_d, _, _, b_fp64 = run_fit_steps(eng, api.PREC_FP64, args.chains, 256, args.evals_cap,
@@ -356,6 +517,9 @@ def main():
     ok &= c32 < 1e29
     rel = np.abs(c32[ok] - c64[ok]) / np.abs(c64[ok])
     truth_rel = float(abs(c32[-1] - c64[-1]) / abs(c64[-1]))
+
+    # Phase drift of the double-float integration against FP64 over the whole light curve.
+    drift = phase_drift(eng, model, obs, P[-1:] if len(P) else P, P[:7])
 
     # End to end through the C ABI with host buffers: ast_eval_batch, copies included.
     B = 16384
@@ -388,6 +552,10 @@ def main():
                        "l2": "flushed before every timed region (256 MB write); simplex state ~100 MB, obs in smem"},
             "fits_per_s": value / args.evals_cap,
             "fp64": {"value": fp64, "unit": UNIT, "speedup_mixed_over_fp64": (value / fp64) if fp64 else None},
+            "batched": None if batched is None else {
+                "value": batched, "unit": UNIT, "speedup_over_fp64": (batched / fp64) if fp64 else None,
+                "path": "ast_batch_step: the workload as one object of the multi-object batch engine"},
+            "phase_drift": drift,
             "accuracy": {"vectors": int(ok.sum()), "of": int(len(P)), "median_rel_dchi2": float(np.median(rel)),
                          "p99_rel_dchi2": float(np.quantile(rel, 0.99)), "max_rel_dchi2": float(rel.max()),
                          "frac_le_1e-6": float(np.mean(rel <= 1e-6)), "true_model_rel_dchi2": truth_rel,

@@ -212,6 +212,11 @@ int ast_eval_batch_device(ast_ctx* ctx, int32_t precision, const double* d_param
  * the model-curve path of the plot mode and of the synthetic-data generator. */
 int ast_model_curve(ast_ctx* ctx, const double* params, double* vmod);
 
+/* Euler angles (phi, theta, psi) at every observation, angles[3*i + k], as integrated by the
+ * FP64 path or by the mixed path (double-float state, reduced to [-pi, pi] at each
+ * observation): the phase drift of the mixed path.  No reference counterpart. */
+int ast_model_angles(ast_ctx* ctx, int32_t precision, const double* params, double* angles);
+
 typedef struct ast_fit_cfg {
     uint64_t seed;          /* -seed; chains draw from Philox4x32-10 keyed by (seed, chain) */
     int64_t  n_chains;      /* N_BLOCKS*BSIZE in the reference */
@@ -315,10 +320,15 @@ int ast_batch_create(int32_t device, int32_t precision, int32_t acc, int64_t n_s
 int ast_batch_add(ast_batch* batch, const ast_model* model, const ast_obs_set* obs, const ast_fit_cfg* cfg,
                   int32_t* index);
 /* Autotuner: times every (tpb, refill) candidate on this batch with bounded launches of
- * evals_per_slot evaluations per slot, keeps the fastest for ast_batch_run and returns it. */
+ * evals_per_slot evaluations per slot, keeps the fastest for ast_batch_run / ast_batch_step and
+ * returns it.  Call it before those: it leaves the batch in its initial state. */
 int ast_batch_tune(ast_batch* batch, int64_t evals_per_slot, ast_batch_launch* best);
 /* Run every chain of every object to completion (tune NULL: the tuned or default geometry). */
 int ast_batch_run(ast_batch* batch, const ast_batch_launch* tune, double* kernel_ms);
+/* Alternatively, advance the batch in bounded launches of evals_per_slot evaluations per slot
+ * (no graph; *done = 1 once every chain has finished and the results are in).  The batch runs
+ * once: either ast_batch_run or ast_batch_step to completion. */
+int ast_batch_step(ast_batch* batch, int64_t evals_per_slot, int32_t* done, double* kernel_ms);
 /* Results of object index, laid out as ast_fit_out of ast_fit (n_evals not filled). */
 int ast_batch_result(ast_batch* batch, int32_t index, ast_fit_out* out);
 int ast_batch_counters(ast_batch* batch, int64_t* n_evals, int64_t* n_fits, int32_t* tpb, int32_t* refill,
