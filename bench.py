@@ -40,6 +40,16 @@ METRIC = "chi2_evals_per_s"
 UNIT = "evals/s"
 
 
+# Executed work per evaluation on the config-2 workload, from ncu captures of the fit kernels
+# (profiles/fit_kernel_mixed_c2.md, profiles/fit_kernel_fp64_c2.md): FP32 flops of the mixed
+# path (FFMA x 2 + FADD + FMUL, the double-float formulation's own arithmetic), FP64 flops of the
+# plain path (DFMA x 2 + DADD + DMUL, including the FP64 transcendental functions), and DRAM bytes
+# of one launch over 38 912 slots (the slot state in and out; independent of the evaluations per
+# slot).  Other workloads scale the per-evaluation figures by their RK4 step count.
+NCU_C2 = {"rk4_steps": 12568, "mixed_fp32_flops": 3.497e7, "fp64_flops": 7.75e6,
+          "slots": 38912, "dram_bytes_mixed": 1.084e8, "dram_bytes_fp64": 7.91e7}
+
+
 def rk4_steps(obs, time_step):
     return int(np.sum(np.floor(np.diff(obs.mjd) / time_step + 1)))
 
@@ -534,7 +544,10 @@ def main():
 
     peak32 = api.probe_peak("fp32", local)
     peak64 = api.probe_peak("fp64", local)
-    achieved = flops * value / 1e9 / max(world, 1)
+    scale = n_rk4 / NCU_C2["rk4_steps"]
+    slots = eng.fit_slots() or NCU_C2["slots"]
+    achieved = NCU_C2["mixed_fp32_flops"] * scale * value / 1e12 / max(world, 1)
+    achieved64 = NCU_C2["fp64_flops"] * scale * fp64 / 1e12 / max(world, 1) if fp64 else None
     cpu = cpu_baseline(model, obs, args.cpu_seconds, s.params_true) if (rank == 0 and world == 1) else None
     clocks = clk.summary()
 
@@ -542,7 +555,8 @@ def main():
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_m / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 rhs/brightness + f64 state (mixed)", "data": "synthetic",
+            "vs_baseline": None, "dtype": "f32 (double-float state and RHS, f32 brightness; f64 set-up and chi2 sums)",
+            "data": "synthetic",
             "config": {"workload": f"{args.config}: {obs.n_data} points, {obs.n_filters} filters, "
                                    f"{api.flag_names(model.flags)}, TIME_STEP {model.time_step}, "
                                    f"{args.chains} chains x {args.evals_cap} evals"
@@ -562,11 +576,21 @@ def main():
                          "nudge_flips": flips,
                          "note": "mixed vs FP64 on sampled vectors whose FP64 chi2 is stable to a one-ulp move of "
                                  "the parameters (cond <= 1e-10)"},
-            "roofline": {"bound": "fp32-pipe (CUDA cores)", "achieved": achieved, "peak": peak32 / 1e3 * 1e3,
-                         "unit": "GFLOP/s", "frac": achieved / peak32, "traffic": None,
-                         "flops_per_eval": flops, "transcendentals_per_eval": trans,
-                         "peak_source": "measured in this run by ast_probe_peak (FP32 FMA loop over every SM)",
-                         "fp64_peak_gflops": peak64},
+            "roofline": {"bound": "fp32 pipe (CUDA cores)", "achieved": achieved, "peak": peak32 / 1e3,
+                         "unit": "TFLOP/s", "frac": achieved / (peak32 / 1e3),
+                         "traffic": NCU_C2["dram_bytes_mixed"] * slots / NCU_C2["slots"],
+                         "kernel": "fit_kernel<double, MIXED>",
+                         "per_eval": {"fp32_flops": NCU_C2["mixed_fp32_flops"] * scale,
+                                      "source": "ncu FFMA x 2 + FADD + FMUL per evaluation "
+                                                "(profiles/fit_kernel_mixed_c2.md)"},
+                         "reference_flops_per_eval": flops, "reference_gflops": flops * value / 1e9,
+                         "transcendentals_per_eval": trans,
+                         "peak_source": "measured in this run by ast_probe_peak (FP32 FMA loop over every SM); "
+                                        "MEASURED_PEAKS.json holds HBM and bf16 only",
+                         "fp64_path": {"kernel": "fit_kernel<double, FP64>", "bound": "fp64 pipe",
+                                       "achieved": achieved64, "peak": peak64 / 1e3, "unit": "TFLOP/s",
+                                       "frac": (achieved64 / (peak64 / 1e3)) if achieved64 else None,
+                                       "per_eval_fp64_flops": NCU_C2["fp64_flops"] * scale}},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": B * model.n_params * 8,
                     "d2h_bytes_per_step": B * (1 + obs.n_filters) * 8, "path": "ast_eval_batch, mixed, host buffers"},

@@ -233,12 +233,14 @@ class RefKernel:
         chi2 = np.zeros(n)
         dv = np.zeros((n, obs.n_filters))
         V = C.c_void_p
+        ms = C.c_double(0)
         rc = self.lib.refk_eval_batch(
             str(self.cubin).encode(), obs_bytes, model.n_params, V(P.ctypes.data), n, V(types.ctypes.data),
             model.n_types, obs.n_data, obs.n_filters, V(obs.mjd.ctypes.data), V(obs.v.ctypes.data),
             V(obs.w.ctypes.data), V(obs.filt.ctypes.data), V(obs.e_unit.ctypes.data), V(obs.s_unit.ctypes.data),
             V(eph.ctypes.data), int(obs.t_min.size), V(obs.t_min.ctypes.data), V(obs.v_min.ctypes.data),
-            V(chi2.ctypes.data), V(dv.ctypes.data))
+            V(chi2.ctypes.data), V(dv.ctypes.data), C.byref(ms))
         if rc:
             raise RuntimeError(self.lib.refk_last_error().decode())
+        self.last_ms = ms.value  # device time of the evaluation launch
         return chi2, dv

@@ -34,7 +34,7 @@ extern "C" int refk_eval_batch(const char* cubin, int obs_bytes, int n_params, c
                                const int* types, int n_types, int n_data, int n_filters, const double* mjd,
                                const float* v, const float* w, const int* filt, const double* e_unit,
                                const double* s_unit, const double* eph21, int n_min, const float* t_min,
-                               const float* v_min, double* chi2_out, double* dv_out)
+                               const float* v_min, double* chi2_out, double* dv_out, double* kernel_ms)
 {
     int rc = 0;
     CUdevice dev;
@@ -85,7 +85,18 @@ extern "C" int refk_eval_batch(const char* cubin, int obs_bytes, int n_params, c
     {
         int nv = n, nd = n_data, nf = n_filters, nm = n_min;
         void* args[] = {&d_p, &nv, &d_types, &d_obs, &nd, &nf, &d_eph, &nm, &d_tmin, &d_vmin, &d_chi2, &d_dv};
+        CUevent e0 = nullptr, e1 = nullptr;
+        CK(cuEventCreate(&e0, CU_EVENT_DEFAULT));
+        CK(cuEventCreate(&e1, CU_EVENT_DEFAULT));
+        CK(cuEventRecord(e0, nullptr));
         CK(cuLaunchKernel(feval, (n + 63) / 64, 1, 1, 64, 1, 1, 0, nullptr, args, nullptr));
+        CK(cuEventRecord(e1, nullptr));
+        CK(cuEventSynchronize(e1));
+        float ms = 0;
+        CK(cuEventElapsedTime(&ms, e0, e1));
+        if (kernel_ms) *kernel_ms = ms;
+        cuEventDestroy(e0);
+        cuEventDestroy(e1);
     }
     CK(cuCtxSynchronize());
     CK(cuMemcpyDtoH(chi2_out, d_chi2, sizeof(double) * n));

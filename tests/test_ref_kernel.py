@@ -90,3 +90,50 @@ def test_fp64_matches_reference_kernel_on_configs(gpu, oracle_mod, synth_objects
     assert not nfin.any()
     assert np.all(rel <= bound), f"max rel {rel.max():.3e}"
     assert np.mean(rel <= RTOL) >= 0.8
+
+
+def test_throughput_against_the_reference_kernel_on_c2(gpu, oracle_mod, synth_objects):
+    """The reference's own chi2one (sm_100 build, one thread per vector) and the two paths here on
+    the same 38 912 config-2 vectors near the true model, each timed by CUDA events around its
+    evaluation launch.  Printed for the record; asserted only loosely (same FP64 arithmetic:
+    the plain path must not be slower than half the reference kernel; the mixed path must beat
+    both)."""
+    import torch
+
+    cubin = REF / "ref_c2_nudge_acc.cubin"
+    if not cubin.exists():
+        pytest.skip(f"{cubin.name} not built (needs the reference checkout where the tree was prepared)")
+    s = synth_objects("c2")
+    m = s.model
+    rng = np.random.default_rng(31)
+    x0 = api.params2x(m, s.params_true)
+    P = []
+    while len(P) < 38912:
+        p = api.x2params(m, x0 + rng.uniform(-0.02, 0.02, m.n_params), reopt=1)
+        if p is not None:
+            P.append(p)
+    P = np.array(P)
+    rk = oracle_mod.RefKernel("c2_nudge_acc")
+    rk.chi2_batch(m, s.obs, P[:256])
+    rk.chi2_batch(m, s.obs, P)
+    ref_rate = len(P) / (rk.last_ms * 1e-3)
+    rates = {}
+    with api.Engine(m, s.obs) as eng:
+        dev = torch.device("cuda:0")
+        dp = torch.from_numpy(P).to(dev)
+        dc = torch.zeros(len(P), dtype=torch.float64, device=dev)
+        dd = torch.zeros(len(P) * s.obs.n_filters, dtype=torch.float64, device=dev)
+        stream = torch.cuda.ExternalStream(eng.stream)
+        for name, prec in (("fp64", api.PREC_FP64), ("mixed", api.PREC_MIXED)):
+            eng.eval_device(dp.data_ptr(), 256, dc.data_ptr(), dd.data_ptr(), eng.stream, prec)
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            eng.eval_device(dp.data_ptr(), len(P), dc.data_ptr(), dd.data_ptr(), eng.stream, prec)
+            b.record(stream)
+            torch.cuda.synchronize()
+            rates[name] = len(P) / (a.elapsed_time(b) * 1e-3)
+    print(f"c2 chi2 evals/s on {len(P)} vectors: reference kernel {ref_rate:.4g}, FP64 {rates['fp64']:.4g} "
+          f"({rates['fp64'] / ref_rate:.2f}x), mixed {rates['mixed']:.4g} ({rates['mixed'] / ref_rate:.2f}x)")
+    assert rates["fp64"] >= 0.5 * ref_rate
+    assert rates["mixed"] > max(rates["fp64"], ref_rate)
