@@ -12,7 +12,7 @@
 // sincos of a double-float angle: Cody-Waite reduction by 2*pi/TABLE with a three-float
 // constant, a TABLE-point table of sin/cos of k*2*pi/TABLE held as double-floats in shared
 // memory, and short series for the remainder |e| <= pi/TABLE, in which only the leading terms
-// are carried as double-floats.  Absolute error < 1e-13 for angles up to ~2e7 rad.
+// are carried as double-floats.  Absolute error ~1e-13 (the e^3/6 term of sin e in FP32).
 //
 // The same code compiles for the host (used to test the arithmetic against FP64): there the
 // operations map to IEEE round-to-nearest float arithmetic (compile with -ffp-contract=off).
@@ -322,13 +322,6 @@ AST_HD df df_log(df x)
     const df lm = df_mul(df{2.0f * r.hi, 2.0f * r.lo}, w);
     const df LN2{0.6931472f, -1.9046542e-09f};
     return df_add(df_mul_f(LN2, (float)e), lm);
-}
-
-// Angle reduced to [-pi, pi] as a float (for FP32 sin/cos in the brightness model).
-AST_HD float df_reduce_f(df a)
-{
-    const df e = df_reduce_2pi(a);
-    return DF_ADD(e.hi, e.lo);
 }
 
 }  // namespace ast

@@ -68,61 +68,6 @@ AST_HD float ls_magnitude_f(float Sb, float Sc, float Sa, float Eb, float Ec, fl
     return -2.5f * log10f(bc * sS * sE / scalar * B);
 }
 
-// FP64 model magnitude at observation i for Euler angles ang = (phi, theta, psi), with the
-// reference's expressions (cuda.c:195-217, 432-689).  Used by the mixed path only where the
-// NUDGE minimum detection needs magnitudes exact to FP64 rounding.
-AST_HD double vmod_fp64(const DevModel& M, const ObsView& o, const double* params, const double* ang, int i)
-{
-    const ast_type_ids& T = M.t;
-#define AST_Q(tt) params[M.idx[T.tt]]
-    const double th_M = AST_Q(theta_M), ph_M = AST_Q(phi_M);
-    const double M_x = sin(th_M) * cos(ph_M), M_y = sin(th_M) * sin(ph_M), M_z = cos(th_M);
-    const double XM = sqrt(M_z * M_z + M_x * M_x);
-    const double XM_x = M_z / XM, XM_z = -M_x / XM;
-    const double YM_x = M_y * XM_z, YM_y = M_z * XM_x - M_x * XM_z, YM_z = -M_y * XM_x;
-    const double cos_phi = cos(ang[0]), sin_phi = sin(ang[0]);
-    const double N_x = XM_x * cos_phi + YM_x * sin_phi, N_y = YM_y * sin_phi, N_z = XM_z * cos_phi + YM_z * sin_phi;
-    const double p_x = N_y * M_z - N_z * M_y, p_y = N_z * M_x - N_x * M_z, p_z = N_x * M_y - N_y * M_x;
-    const double cos_theta = cos(ang[1]), sin_theta = sin(ang[1]);
-    double a_x = M_x * cos_theta + p_x * sin_theta, a_y = M_y * cos_theta + p_y * sin_theta,
-           a_z = M_z * cos_theta + p_z * sin_theta;
-    const double w_x = a_y * N_z - a_z * N_y, w_y = a_z * N_x - a_x * N_z, w_z = a_x * N_y - a_y * N_x;
-    const double sin_psi = sin(ang[2]), cos_psi = cos(ang[2]);
-    const double b_x = N_x * cos_psi + w_x * sin_psi, b_y = N_y * cos_psi + w_y * sin_psi,
-                 b_z = N_z * cos_psi + w_z * sin_psi;
-    const double c_x = a_y * b_z - a_z * b_y, c_y = a_z * b_x - a_x * b_z, c_z = a_x * b_y - a_y * b_x;
-    const double E_x1 = o.ex[i], E_y1 = o.ey[i], E_z1 = o.ez[i], S_x1 = o.sx[i], S_y1 = o.sy[i], S_z1 = o.sz[i];
-    if (M.flags & AST_BW_BALL) {
-        const double cR = cos(AST_Q(phi_R)), sR = sin(AST_Q(phi_R)), cT = cos(AST_Q(theta_R)), sT = sin(AST_Q(theta_R));
-        const double Nx = b_x * cR + c_x * sR, Ny = b_y * cR + c_y * sR, Nz = b_z * cR + c_z * sR;
-        const double px = Ny * a_z - Nz * a_y, py = Nz * a_x - Nx * a_z, pz = Nx * a_y - Ny * a_x;
-        a_x = a_x * cT + px * sT;
-        a_y = a_y * cT + py * sT;
-        a_z = a_z * cT + pz * sT;
-        const double cos_zeta = a_x * E_x1 + a_y * E_y1 + a_z * E_z1;
-        return -2.5 * log10(0.5 * (AST_Q(kappa) * (1 + cos_zeta) + 0.5 * (1 - cos_zeta)));
-    }
-    const double Ep_b = b_x * E_x1 + b_y * E_y1 + b_z * E_z1, Ep_c = c_x * E_x1 + c_y * E_y1 + c_z * E_z1,
-                 Ep_a = a_x * E_x1 + a_y * E_y1 + a_z * E_z1;
-    const double Sp_b = b_x * S_x1 + b_y * S_y1 + b_z * S_z1, Sp_c = c_x * S_x1 + c_y * S_y1 + c_z * S_z1,
-                 Sp_a = a_x * S_x1 + a_y * S_y1 + a_z * S_z1;
-    const double b = (M.flags & AST_BC) ? AST_Q(b) : AST_Q(b_tumb);
-    const double c = (M.flags & AST_BC) ? AST_Q(c) : AST_Q(c_tumb);
-#undef AST_Q
-    const double scalar_Sun = sqrt(Sp_b * Sp_b / (b * b) + Sp_c * Sp_c / (c * c) + Sp_a * Sp_a);
-    const double scalar_Earth = sqrt(Ep_b * Ep_b / (b * b) + Ep_c * Ep_c / (c * c) + Ep_a * Ep_a);
-    const double cos_alpha_p = (Sp_b * Ep_b / (b * b) + Sp_c * Ep_c / (c * c) + Sp_a * Ep_a) / (scalar_Sun * scalar_Earth);
-    const double sin_alpha_p = sqrt(1.0 - cos_alpha_p * cos_alpha_p);
-    const double alpha_p = atan2(sin_alpha_p, cos_alpha_p);
-    const double scalar = sqrt(scalar_Sun * scalar_Sun + scalar_Earth * scalar_Earth + 2 * scalar_Sun * scalar_Earth * cos_alpha_p);
-    const double cos_lambda_p = (scalar_Sun + scalar_Earth * cos_alpha_p) / scalar;
-    const double sin_lambda_p = scalar_Earth * sin_alpha_p / scalar;
-    const double lambda_p = atan2(sin_lambda_p, cos_lambda_p);
-    return -2.5 * log10(b * c * scalar_Sun * scalar_Earth / scalar *
-                        (cos(lambda_p - alpha_p) + cos_lambda_p +
-                         sin_lambda_p * sin(lambda_p - alpha_p) * log(1.0 / tan(0.5 * lambda_p) / tan(0.5 * (alpha_p - lambda_p)))));
-}
-
 // sin and cos of two double-float angles through one copy of df_sincos (a rolled loop keeps
 // the right-hand side small enough for the instruction cache).
 AST_HD void df_sincos2(df a0, df a1, const float4* tab, df* s0, df* c0, df* s1, df* c1)
@@ -275,6 +220,41 @@ struct DfFrame {
     df cR, sR, cT, sT, kappa;
 };
 
+// The per-evaluation constants of vmod_df for parameter vector params (cuda.c:195-217, 568-574).
+AST_HD DfFrame make_df_frame(const DevModel& M, const double* params)
+{
+    const ast_type_ids& T = M.t;
+#define AST_Q(tt) params[M.idx[T.tt]]
+    const double th_M = AST_Q(theta_M), ph_M = AST_Q(phi_M);
+    const double Mx = sin(th_M) * cos(ph_M), My = sin(th_M) * sin(ph_M), Mz = cos(th_M);
+    const double XM = sqrt(Mz * Mz + Mx * Mx);
+    const double XMx = Mz / XM, XMz = -Mx / XM;
+    DfFrame F;
+    F.M[0] = df_from_double(Mx);
+    F.M[1] = df_from_double(My);
+    F.M[2] = df_from_double(Mz);
+    F.XM_x = df_from_double(XMx);
+    F.XM_z = df_from_double(XMz);
+    F.YM[0] = df_from_double(My * XMz);
+    F.YM[1] = df_from_double(Mz * XMx - Mx * XMz);
+    F.YM[2] = df_from_double(-My * XMx);
+    if (M.flags & AST_BW_BALL) {
+        F.kappa = df_from_double(AST_Q(kappa));
+        F.cR = df_from_double(cos(AST_Q(phi_R)));
+        F.sR = df_from_double(sin(AST_Q(phi_R)));
+        F.cT = df_from_double(cos(AST_Q(theta_R)));
+        F.sT = df_from_double(sin(AST_Q(theta_R)));
+    } else {
+        const double b = (M.flags & AST_BC) ? AST_Q(b) : AST_Q(b_tumb);
+        const double c = (M.flags & AST_BC) ? AST_Q(c) : AST_Q(c_tumb);
+        F.ib = df_from_double(1.0 / b);
+        F.ic = df_from_double(1.0 / c);
+        F.bc = df_from_double(b * c);
+    }
+#undef AST_Q
+    return F;
+}
+
 // Model magnitude at observation i for the double-float Euler angles ang = (phi, theta, psi):
 // the body frame as in cuda.c:432-473, then ls_magnitude_df or the BW_BALL law (cuda.c:568-580).
 AST_HD double vmod_df(const DevModel& M, const ObsView& o, const DfFrame& F, const df* ang, int i, const float4* tab)
@@ -423,29 +403,7 @@ __host__ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const dou
     }
     const float ib = 1.0f / b_ph, ic = 1.0f / c_ph;
     DfFrame F;
-    if (flags & AST_NUDGE) {
-        F.M[0] = df_from_double(M_xd);
-        F.M[1] = df_from_double(M_yd);
-        F.M[2] = df_from_double(M_zd);
-        F.XM_x = df_from_double(M_zd / XMd);
-        F.XM_z = df_from_double(-M_xd / XMd);
-        F.YM[0] = df_from_double(M_yd * (-M_xd / XMd));
-        F.YM[1] = df_from_double(M_zd * (M_zd / XMd) - M_xd * (-M_xd / XMd));
-        F.YM[2] = df_from_double(-M_yd * (M_zd / XMd));
-        if (bw) {
-            F.kappa = df_from_double(AST_P(kappa));
-            F.cR = df_from_double(cos(AST_P(phi_R)));
-            F.sR = df_from_double(sin(AST_P(phi_R)));
-            F.cT = df_from_double(cos(AST_P(theta_R)));
-            F.sT = df_from_double(sin(AST_P(theta_R)));
-        } else {
-            const double bb = (flags & AST_BC) ? AST_P(b) : bt, cc = (flags & AST_BC) ? AST_P(c) : ct;
-            F.ib = df_from_double(1.0 / bb);
-            F.ic = df_from_double(1.0 / cc);
-            F.bc = df_from_double(bb * cc);
-        }
-    }
-
+    if (flags & AST_NUDGE) F = make_df_frame(M, params);
     for (int i = 0; i < N_data; i++) {
         if (i > 0) {
             const int N_steps = o.nst[i];
