@@ -41,7 +41,7 @@ extern "C" {
 #define AST_NOBS_MAX     10   /* observed minima, asteroid.h:219 */
 #define AST_M_MAX        30   /* model minima, asteroid.h:217 */
 #define AST_N_COLUMNS    6
-#define AST_MAX_DATA     16384 /* observations per object (staged tile-wise when large) */
+#define AST_MAX_DATA     16384 /* observations per object (MAX_DATA, asteroid.h; a run-time limit here) */
 
 /* ---------------------------------------------------------------- status codes */
 #define AST_OK             0
