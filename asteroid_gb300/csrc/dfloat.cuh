@@ -39,6 +39,10 @@ __device__ __forceinline__ float df_rcp_approx(float a)
     return r;
 }
 #define DF_RCP_APPROX(a) df_rcp_approx(a)
+#define DD_ADD(a, b) __dadd_rn(a, b)
+#define DD_SUB(a, b) __dsub_rn(a, b)
+#define DD_MUL(a, b) __dmul_rn(a, b)
+#define DD_FMA(a, b, c) __fma_rn(a, b, c)
 #else
 static inline float df_h_add(float a, float b) { volatile float r = a + b; return r; }
 static inline float df_h_sub(float a, float b) { volatile float r = a - b; return r; }
@@ -51,10 +55,29 @@ static inline int df_h_bits(float a) { int i; memcpy(&i, &a, 4); return i; }
 #define DF_FMA(a, b, c) fmaf(a, b, c)
 #define DF_RCP(a) df_h_rcp(a)
 #define DF_RCP_APPROX(a) df_h_rcp(a)
+static inline double dd_h_add(double a, double b) { volatile double r = a + b; return r; }
+static inline double dd_h_sub(double a, double b) { volatile double r = a - b; return r; }
+static inline double dd_h_mul(double a, double b) { volatile double r = a * b; return r; }
+#define DD_ADD(a, b) dd_h_add(a, b)
+#define DD_SUB(a, b) dd_h_sub(a, b)
+#define DD_MUL(a, b) dd_h_mul(a, b)
+#define DD_FMA(a, b, c) fma(a, b, c)
 #define DF_BITS(a) df_h_bits(a)
 #endif
 
 namespace ast {
+
+// Single operations with their rounding spelled out.  Code built from these gives the same bits
+// wherever the compiler inlines it: a free expression such as a*b + c*d may be fused into a
+// multiply-add on either product, and which one can depend on the surrounding kernel.
+AST_HD float f_dot2(float a, float b, float c, float d) { return DF_FMA(a, b, DF_MUL(c, d)); }   // ab + cd
+AST_HD float f_dif2(float a, float b, float c, float d) { return DF_FMA(a, b, -DF_MUL(c, d)); }  // ab - cd
+AST_HD float f_dot3(float a, float b, float c, float d, float e, float f)
+{
+    return DF_FMA(a, b, DF_FMA(c, d, DF_MUL(e, f)));
+}
+AST_HD double d_dot2(double a, double b, double c, double d) { return DD_FMA(a, b, DD_MUL(c, d)); }
+AST_HD double d_dif2(double a, double b, double c, double d) { return DD_FMA(a, b, -DD_MUL(c, d)); }
 
 struct df {
     float hi, lo;

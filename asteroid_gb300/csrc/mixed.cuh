@@ -21,7 +21,7 @@ namespace ast {
 // sum_k 2 t^(2k+1) / ((2k-1)(2k+1)), else the closed form (cancellation at most 6x there).
 AST_HD float ls_f(float t)
 {
-    const float t2 = t * t;
+    const float t2 = DF_MUL(t, t);
     if (t < 0.5f) {
         float p = 2.0f / 575.0f;  // k = 12
         p = fmaf(p, t2, 2.0f / 483.0f);
@@ -35,9 +35,10 @@ AST_HD float ls_f(float t)
         p = fmaf(p, t2, 2.0f / 35.0f);
         p = fmaf(p, t2, 2.0f / 15.0f);
         p = fmaf(p, t2, 2.0f / 3.0f);
-        return p * t2 * t;
+        return DF_MUL(DF_MUL(p, t2), t);
     }
-    return t - (1.0f - t2) * 0.5f * log1pf(2.0f * t / (1.0f - t));
+    const float om = DF_SUB(1.0f, t);
+    return DF_SUB(t, DF_MUL(DF_MUL(DF_SUB(1.0f, t2), 0.5f), log1pf(DF_MUL(2.0f, t) / om)));
 }
 
 // Lommel-Seeliger ellipsoid magnitude, Muinonen & Lumme (2015) eqs. 10-14 as in cuda.c:664-689,
@@ -51,21 +52,21 @@ AST_HD float ls_f(float t)
 //    = 2 D^2 f(s/D), D = cos((mu - nu)/2), s = cos((mu + nu)/2), f as in ls_f.
 AST_HD float ls_magnitude_f(float Sb, float Sc, float Sa, float Eb, float Ec, float Ea, float ib, float ic, float bc)
 {
-    const float sx = Sb * ib, sy = Sc * ic, sz = Sa;
-    const float ex = Eb * ib, ey = Ec * ic, ez = Ea;
-    const float hx = (Sb + Eb) * ib, hy = (Sc + Ec) * ic, hz = Sa + Ea;
-    const float sS = sqrtf(sx * sx + sy * sy + sz * sz);
-    const float sE = sqrtf(ex * ex + ey * ey + ez * ez);
-    const float scalar = sqrtf(hx * hx + hy * hy + hz * hz);
-    const float cx = sy * ez - sz * ey, cy = sz * ex - sx * ez, cz = sx * ey - sy * ex;
-    const float cn = sqrtf(cx * cx + cy * cy + cz * cz);  // |S' x E'| = |S' x H'| = |H' x E'|
-    const float mu = atan2f(cn, sx * hx + sy * hy + sz * hz);
-    const float nu = atan2f(cn, hx * ex + hy * ey + hz * ez);
-    const float D = cosf(0.5f * (mu - nu));
+    const float sx = DF_MUL(Sb, ib), sy = DF_MUL(Sc, ic), sz = Sa;
+    const float ex = DF_MUL(Eb, ib), ey = DF_MUL(Ec, ic), ez = Ea;
+    const float hx = DF_MUL(DF_ADD(Sb, Eb), ib), hy = DF_MUL(DF_ADD(Sc, Ec), ic), hz = DF_ADD(Sa, Ea);
+    const float sS = sqrtf(f_dot3(sx, sx, sy, sy, sz, sz));
+    const float sE = sqrtf(f_dot3(ex, ex, ey, ey, ez, ez));
+    const float scalar = sqrtf(f_dot3(hx, hx, hy, hy, hz, hz));
+    const float cx = f_dif2(sy, ez, sz, ey), cy = f_dif2(sz, ex, sx, ez), cz = f_dif2(sx, ey, sy, ex);
+    const float cn = sqrtf(f_dot3(cx, cx, cy, cy, cz, cz));  // |S' x E'| = |S' x H'| = |H' x E'|
+    const float mu = atan2f(cn, f_dot3(sx, hx, sy, hy, sz, hz));
+    const float nu = atan2f(cn, f_dot3(hx, ex, hy, ey, hz, ez));
+    const float D = cosf(DF_MUL(0.5f, DF_SUB(mu, nu)));
     // s = cos(alpha'/2) = sin(eps/2) with eps = pi - alpha' taken directly from the vectors.
-    const float s = sinf(0.5f * atan2f(cn, -(sx * ex + sy * ey + sz * ez)));
-    const float B = 2.0f * D * D * ls_f(s / D);
-    return -2.5f * log10f(bc * sS * sE / scalar * B);
+    const float s = sinf(DF_MUL(0.5f, atan2f(cn, -f_dot3(sx, ex, sy, ey, sz, ez))));
+    const float B = DF_MUL(DF_MUL(DF_MUL(2.0f, D), D), ls_f(s / D));
+    return DF_MUL(-2.5f, log10f(DF_MUL(DF_MUL(DF_MUL(bc, sS), sE) / scalar, B)));
 }
 
 // sin and cos of two double-float angles through one copy of df_sincos (a rolled loop keeps
@@ -226,8 +227,8 @@ AST_HD DfFrame make_df_frame(const DevModel& M, const double* params)
     const ast_type_ids& T = M.t;
 #define AST_Q(tt) params[M.idx[T.tt]]
     const double th_M = AST_Q(theta_M), ph_M = AST_Q(phi_M);
-    const double Mx = sin(th_M) * cos(ph_M), My = sin(th_M) * sin(ph_M), Mz = cos(th_M);
-    const double XM = sqrt(Mz * Mz + Mx * Mx);
+    const double Mx = DD_MUL(sin(th_M), cos(ph_M)), My = DD_MUL(sin(th_M), sin(ph_M)), Mz = cos(th_M);
+    const double XM = sqrt(d_dot2(Mz, Mz, Mx, Mx));
     const double XMx = Mz / XM, XMz = -Mx / XM;
     DfFrame F;
     F.M[0] = df_from_double(Mx);
@@ -235,9 +236,9 @@ AST_HD DfFrame make_df_frame(const DevModel& M, const double* params)
     F.M[2] = df_from_double(Mz);
     F.XM_x = df_from_double(XMx);
     F.XM_z = df_from_double(XMz);
-    F.YM[0] = df_from_double(My * XMz);
-    F.YM[1] = df_from_double(Mz * XMx - Mx * XMz);
-    F.YM[2] = df_from_double(-My * XMx);
+    F.YM[0] = df_from_double(DD_MUL(My, XMz));
+    F.YM[1] = df_from_double(d_dif2(Mz, XMx, Mx, XMz));
+    F.YM[2] = df_from_double(-DD_MUL(My, XMx));
     if (M.flags & AST_BW_BALL) {
         F.kappa = df_from_double(AST_Q(kappa));
         F.cR = df_from_double(cos(AST_Q(phi_R)));
@@ -249,7 +250,7 @@ AST_HD DfFrame make_df_frame(const DevModel& M, const double* params)
         const double c = (M.flags & AST_BC) ? AST_Q(c) : AST_Q(c_tumb);
         F.ib = df_from_double(1.0 / b);
         F.ic = df_from_double(1.0 / c);
-        F.bc = df_from_double(b * c);
+        F.bc = df_from_double(DD_MUL(b, c));
     }
 #undef AST_Q
     return F;
@@ -321,11 +322,12 @@ static __host__ __device__ __noinline__ bool nudge_flush(const DevModel& M, cons
             const float t0 = (float)o.t[ic - 2], t1 = (float)o.t[ic - 1];
             const double ti = o.t[ic];
             const double a = ((v2 - f1) / (ti - t1) - (f1 - f0) / (t1 - t0)) / (ti - t0);
-            const double b = (f1 - f0) / (t1 - t0) - a * (t1 + t0);
-            const double c = f1 - a * t1 * t1 - b * t1;
+            const double b = DD_SUB((f1 - f0) / (t1 - t0), DD_MUL(a, (double)DF_ADD(t1, t0)));
+            const double c = DD_SUB(DD_SUB(f1, DD_MUL(DD_MUL(a, t1), t1)), DD_MUL(b, t1));
             const int m = *Mmin - 1;
             t_mod[m] = (float)(-b / 2.0 / a);
-            V_mod[m] = (float)(a * t_mod[m] * t_mod[m] + b * t_mod[m] + c);
+            const double tm = t_mod[m];
+            V_mod[m] = (float)DD_ADD(DD_ADD(DD_MUL(DD_MUL(a, tm), tm), DD_MUL(b, tm)), c);
         }
     }
     *n_cand = 0;
@@ -353,39 +355,44 @@ __host__ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const dou
 #define AST_P(tt) params[M.idx[T.tt]]
     // Per-evaluation set-up in FP64.
     const double th_M = AST_P(theta_M), ph_M = AST_P(phi_M);
-    const double M_xd = sin(th_M) * cos(ph_M), M_yd = sin(th_M) * sin(ph_M), M_zd = cos(th_M);
-    const double XMd = sqrt(M_zd * M_zd + M_xd * M_xd);
+    // Every rounding explicit (DD_*, DF_*, f_*, d_*), with float and double operands as in the
+    // reference's expressions: the same bits in every kernel that inlines this function.
+    const double M_xd = DD_MUL(sin(th_M), cos(ph_M)), M_yd = DD_MUL(sin(th_M), sin(ph_M)), M_zd = cos(th_M);
+    const double XMd = sqrt(d_dot2(M_zd, M_zd, M_xd, M_xd));
     const float M_x = (float)M_xd, M_y = (float)M_yd, M_z = (float)M_zd;
     const float XM_x = (float)(M_zd / XMd), XM_z = (float)(-M_xd / XMd);
-    const float YM_x = M_y * XM_z, YM_y = M_z * XM_x - M_x * XM_z, YM_z = -M_y * XM_x;
+    const float YM_x = DF_MUL(M_y, XM_z), YM_y = f_dif2(M_z, XM_x, M_x, XM_z), YM_z = -DF_MUL(M_y, XM_x);
     const double bt = AST_P(b_tumb), ct = AST_P(c_tumb);
-    const double Is = (1.0 + bt * bt) / (bt * bt + ct * ct);
-    const double Ii = (1.0 + ct * ct) / (bt * bt + ct * ct);
+    const double bt2 = DD_MUL(bt, bt), ct2 = DD_MUL(ct, ct);
+    const double Is = DD_ADD(1.0, bt2) / DD_ADD(bt2, ct2);
+    const double Ii = DD_ADD(1.0, ct2) / DD_ADD(bt2, ct2);
     const double Is_inv = 1.0 / Is, Ii_inv = 1.0 / Ii;
     const double psi0 = AST_P(psi_0);
     df y[6];
     df mu[6];
     const bool torque = (flags & AST_TORQUE) != 0;
     {
-        const double theta = asin(sqrt((AST_P(Es) - 1.0) / (sin(psi0) * sin(psi0) * (Ii_inv - Is_inv) + Is_inv - 1.0)));
+        const double sp = sin(psi0);
+        const double den = DD_SUB(DD_ADD(DD_MUL(DD_MUL(sp, sp), DD_SUB(Ii_inv, Is_inv)), Is_inv), 1.0);
+        const double theta = asin(sqrt(DD_SUB(AST_P(Es), 1.0) / den));
         if (torque) {
-            mu[0] = df_from_double((Is - 1.0) * Ii_inv);
-            mu[1] = df_from_double((1.0 - Ii) * Is_inv);
-            mu[2] = df_from_double(Ii - Is);
+            mu[0] = df_from_double(DD_MUL(DD_SUB(Is, 1.0), Ii_inv));
+            mu[1] = df_from_double(DD_MUL(DD_SUB(1.0, Ii), Is_inv));
+            mu[2] = df_from_double(DD_SUB(Ii, Is));
             mu[3] = df_from_double(AST_P(Ti));
             mu[4] = df_from_double(AST_P(Ts));
             mu[5] = df_from_double(AST_P(Tl));
             const double L = AST_P(L);
-            y[0] = df_from_double(L * Ii_inv * sin(theta) * sin(psi0));
-            y[1] = df_from_double(L * Is_inv * sin(theta) * cos(psi0));
-            y[2] = df_from_double(L * cos(theta));
+            y[0] = df_from_double(DD_MUL(DD_MUL(DD_MUL(L, Ii_inv), sin(theta)), sp));
+            y[1] = df_from_double(DD_MUL(DD_MUL(DD_MUL(L, Is_inv), sin(theta)), cos(psi0)));
+            y[2] = df_from_double(DD_MUL(L, cos(theta)));
             y[3] = df_from_double(AST_P(phi_0));
             y[4] = df_from_double(theta);
             y[5] = df_from_double(psi0);
         } else {
             mu[0] = df_from_double(AST_P(L));
-            mu[1] = df_from_double(0.5 * (Ii_inv + Is_inv));
-            mu[2] = df_from_double(0.5 * (Ii_inv - Is_inv));
+            mu[1] = df_from_double(DD_MUL(0.5, DD_ADD(Ii_inv, Is_inv)));
+            mu[2] = df_from_double(DD_MUL(0.5, DD_SUB(Ii_inv, Is_inv)));
             y[0] = df_from_double(AST_P(phi_0));
             y[1] = df_from_double(theta);
             y[2] = df_from_double(psi0);
@@ -443,47 +450,48 @@ __host__ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const dou
         sincosf(DF_ADD(ang[0].hi, ang[0].lo), &sin_phi, &cos_phi);
         sincosf(DF_ADD(ang[1].hi, ang[1].lo), &sin_theta, &cos_theta);
         sincosf(DF_ADD(ang[2].hi, ang[2].lo), &sin_psi, &cos_psi);
-        float N_x = XM_x * cos_phi + YM_x * sin_phi;
-        float N_y = YM_y * sin_phi;
-        float N_z = XM_z * cos_phi + YM_z * sin_phi;
-        float p_x = N_y * M_z - N_z * M_y;
-        float p_y = N_z * M_x - N_x * M_z;
-        float p_z = N_x * M_y - N_y * M_x;
-        float a_x = M_x * cos_theta + p_x * sin_theta;
-        float a_y = M_y * cos_theta + p_y * sin_theta;
-        float a_z = M_z * cos_theta + p_z * sin_theta;
-        const float w_x = a_y * N_z - a_z * N_y;
-        const float w_y = a_z * N_x - a_x * N_z;
-        const float w_z = a_x * N_y - a_y * N_x;
-        const float b_x = N_x * cos_psi + w_x * sin_psi;
-        const float b_y = N_y * cos_psi + w_y * sin_psi;
-        const float b_z = N_z * cos_psi + w_z * sin_psi;
-        const float c_x = a_y * b_z - a_z * b_y;
-        const float c_y = a_z * b_x - a_x * b_z;
-        const float c_z = a_x * b_y - a_y * b_x;
+        float N_x = f_dot2(XM_x, cos_phi, YM_x, sin_phi);
+        float N_y = DF_MUL(YM_y, sin_phi);
+        float N_z = f_dot2(XM_z, cos_phi, YM_z, sin_phi);
+        float p_x = f_dif2(N_y, M_z, N_z, M_y);
+        float p_y = f_dif2(N_z, M_x, N_x, M_z);
+        float p_z = f_dif2(N_x, M_y, N_y, M_x);
+        float a_x = f_dot2(M_x, cos_theta, p_x, sin_theta);
+        float a_y = f_dot2(M_y, cos_theta, p_y, sin_theta);
+        float a_z = f_dot2(M_z, cos_theta, p_z, sin_theta);
+        const float w_x = f_dif2(a_y, N_z, a_z, N_y);
+        const float w_y = f_dif2(a_z, N_x, a_x, N_z);
+        const float w_z = f_dif2(a_x, N_y, a_y, N_x);
+        const float b_x = f_dot2(N_x, cos_psi, w_x, sin_psi);
+        const float b_y = f_dot2(N_y, cos_psi, w_y, sin_psi);
+        const float b_z = f_dot2(N_z, cos_psi, w_z, sin_psi);
+        const float c_x = f_dif2(a_y, b_z, a_z, b_y);
+        const float c_y = f_dif2(a_z, b_x, a_x, b_z);
+        const float c_z = f_dif2(a_x, b_y, a_y, b_x);
         const float E_x1 = o.efx[i], E_y1 = o.efy[i], E_z1 = o.efz[i];
         const float S_x1 = o.sfx[i], S_y1 = o.sfy[i], S_z1 = o.sfz[i];
         float Vmod;
         if (bw) {
-            N_x = b_x * cos_phR + c_x * sin_phR;
-            N_y = b_y * cos_phR + c_y * sin_phR;
-            N_z = b_z * cos_phR + c_z * sin_phR;
-            p_x = N_y * a_z - N_z * a_y;
-            p_y = N_z * a_x - N_x * a_z;
-            p_z = N_x * a_y - N_y * a_x;
-            a_x = a_x * cos_thR + p_x * sin_thR;
-            a_y = a_y * cos_thR + p_y * sin_thR;
-            a_z = a_z * cos_thR + p_z * sin_thR;
-            const float cos_zeta = a_x * E_x1 + a_y * E_y1 + a_z * E_z1;
-            Vmod = -2.5f * log10f(0.5f * (kappa * (1 + cos_zeta) + 0.5f * (1 - cos_zeta)));
+            N_x = f_dot2(b_x, cos_phR, c_x, sin_phR);
+            N_y = f_dot2(b_y, cos_phR, c_y, sin_phR);
+            N_z = f_dot2(b_z, cos_phR, c_z, sin_phR);
+            p_x = f_dif2(N_y, a_z, N_z, a_y);
+            p_y = f_dif2(N_z, a_x, N_x, a_z);
+            p_z = f_dif2(N_x, a_y, N_y, a_x);
+            a_x = f_dot2(a_x, cos_thR, p_x, sin_thR);
+            a_y = f_dot2(a_y, cos_thR, p_y, sin_thR);
+            a_z = f_dot2(a_z, cos_thR, p_z, sin_thR);
+            const float cos_zeta = f_dot3(a_x, E_x1, a_y, E_y1, a_z, E_z1);
+            const float arg = f_dot2(kappa, DF_ADD(1.0f, cos_zeta), 0.5f, DF_SUB(1.0f, cos_zeta));
+            Vmod = DF_MUL(-2.5f, log10f(DF_MUL(0.5f, arg)));
         } else {
-            const float Ep_b = b_x * E_x1 + b_y * E_y1 + b_z * E_z1;
-            const float Ep_c = c_x * E_x1 + c_y * E_y1 + c_z * E_z1;
-            const float Ep_a = a_x * E_x1 + a_y * E_y1 + a_z * E_z1;
-            const float Sp_b = b_x * S_x1 + b_y * S_y1 + b_z * S_z1;
-            const float Sp_c = c_x * S_x1 + c_y * S_y1 + c_z * S_z1;
-            const float Sp_a = a_x * S_x1 + a_y * S_y1 + a_z * S_z1;
-            Vmod = ls_magnitude_f(Sp_b, Sp_c, Sp_a, Ep_b, Ep_c, Ep_a, ib, ic, b_ph * c_ph);
+            const float Ep_b = f_dot3(b_x, E_x1, b_y, E_y1, b_z, E_z1);
+            const float Ep_c = f_dot3(c_x, E_x1, c_y, E_y1, c_z, E_z1);
+            const float Ep_a = f_dot3(a_x, E_x1, a_y, E_y1, a_z, E_z1);
+            const float Sp_b = f_dot3(b_x, S_x1, b_y, S_y1, b_z, S_z1);
+            const float Sp_c = f_dot3(c_x, S_x1, c_y, S_y1, c_z, S_z1);
+            const float Sp_a = f_dot3(a_x, S_x1, a_y, S_y1, a_z, S_z1);
+            Vmod = ls_magnitude_f(Sp_b, Sp_c, Sp_a, Ep_b, Ep_c, Ep_a, ib, ic, DF_MUL(b_ph, c_ph));
         }
         {
             // Residual and weighted sums as double-floats: v - Vmod exactly (TwoSum), products
@@ -535,7 +543,7 @@ __host__ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const dou
     CF dv[AST_MAX_FILTERS];
     for (int m = 0; m < N_filters; m++) {
         const double sy = df_to_double(sum_y[m]), sy2 = df_to_double(sum_y2[m]), sw = o.sum_w[m];
-        chi2m = (CF)(sy2 - sy * sy / sw);
+        chi2m = (CF)DD_SUB(sy2, DD_MUL(sy, sy) / sw);
         chi2a = chi2a + chi2m;
         dv[m] = (CF)(sy / sw);
     }
@@ -548,14 +556,15 @@ __host__ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const dou
                 if (dt < AST_DT_MAX2) {
                     if (dt > AST_DT_MAX) {
                         const float x = (AST_DT_MAX2 - dt) / (AST_DT_MAX2 - AST_DT_MAX);
-                        S_M = (float)(S_M + x * x * (-2.0 * x + 3.0));
+                        S_M = (float)DD_ADD(S_M, DD_MUL((double)DF_MUL(x, x), DD_ADD(DD_MUL(-2.0, (double)x), 3.0)));
                     } else {
                         S_M = (float)(S_M + 1.0);
                         const float dV = (float)(V_mod[imod] + dv[0] - M.v_min[iobs]);
-                        const float x = sqrtf(dt * dt / AST_DT_MAX / AST_DT_MAX + dV * dV / AST_DV_MAX / AST_DV_MAX);
+                        const float x = sqrtf(DF_ADD(DF_MUL(dt, dt) / AST_DT_MAX / AST_DT_MAX,
+                                                     DF_MUL(dV, dV) / AST_DV_MAX / AST_DV_MAX));
                         if (x < 1.0f) {
-                            const float P_i = AST_L_A * x * x / (x * x + AST_L_RC2);
-                            P_tot = (float)(P_tot * (AST_P_MIN * (1.0 + AST_P_MIN2 * P_i)));
+                            const float P_i = DF_MUL(DF_MUL(AST_L_A, x), x) / DF_ADD(DF_MUL(x, x), AST_L_RC2);
+                            P_tot = (float)DD_MUL(P_tot, DD_MUL(AST_P_MIN, DD_ADD(1.0, (double)DF_MUL(AST_P_MIN2, P_i))));
                         }
                     }
                 }
@@ -567,7 +576,7 @@ __host__ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const dou
             P_tot = 1.0f;
         else if (chi2a > AST_CHI2_0) {
             const float x = (float)((AST_CHI2_1 - chi2a) / (AST_CHI2_1 - AST_CHI2_0));
-            const float beta = x * x * (-2 * x + 3);
+            const float beta = DF_MUL(DF_MUL(x, x), DF_ADD(DF_MUL(-2.0f, x), 3.0f));
             P_tot = powf(P_tot, beta);
         }
         float P_M;
@@ -575,7 +584,7 @@ __host__ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const dou
             P_M = 1.0f;
         else if (S_M < AST_M_MAX) {
             const float x = (S_M - AST_M_MAX2) / (AST_M_MAX - AST_M_MAX2);
-            P_M = (float)(1.0 + 3 * x * x * (-2 * x + 3));
+            P_M = (float)DD_ADD(1.0, (double)DF_MUL(DF_MUL(DF_MUL(3.0f, x), x), DF_ADD(DF_MUL(-2.0f, x), 3.0f)));
         } else
             P_M = 4.0f;
         chi2a = chi2a * P_tot * P_M;
