@@ -263,7 +263,7 @@ class Engine:
         return out
 
     def _cfg(self, n_chains, group_size, n_stages, seed, reopt, params0, precision, evals_cap, steps_cap, tpb,
-             min_ctas_per_sm=0, stage_obs=0):
+             min_ctas_per_sm=0, stage_obs=0, fp64_result=False):
         cfg = capi.FitCfg()
         cfg.seed = int(seed) & ((1 << 64) - 1)
         cfg.n_chains = int(n_chains)
@@ -276,6 +276,7 @@ class Engine:
         cfg.tpb = int(tpb)
         cfg.min_ctas_per_sm = int(min_ctas_per_sm)
         cfg.stage_obs = int(stage_obs)
+        cfg.fp64_result = int(bool(fp64_result))
         self._p0 = None
         if reopt:
             self._p0 = np.ascontiguousarray(params0, dtype=np.float64)
@@ -283,9 +284,10 @@ class Engine:
         return cfg
 
     def fit_begin(self, n_chains=56 * 256, group_size=256, n_stages=1, seed=1, reopt=False, params0=None,
-                  precision=PREC_FP64, evals_cap=0, steps_cap=0, tpb=0, min_ctas_per_sm=0, stage_obs=0):
+                  precision=PREC_FP64, evals_cap=0, steps_cap=0, tpb=0, min_ctas_per_sm=0, stage_obs=0,
+                  fp64_result=False):
         self._fitcfg = self._cfg(n_chains, group_size, n_stages, seed, reopt, params0, precision, evals_cap,
-                                 steps_cap, tpb, min_ctas_per_sm, stage_obs)
+                                 steps_cap, tpb, min_ctas_per_sm, stage_obs, fp64_result)
         check(self.lib.ast_fit_begin(self.ctx, C.byref(self._fitcfg)), "ast_fit_begin")
 
     def fit_step(self, evals_per_slot: int = 0, stream: int = 0) -> bool:
@@ -323,10 +325,11 @@ class Engine:
         return res
 
     def fit(self, n_chains=56 * 256, group_size=256, n_stages=1, seed=1, reopt=False, params0=None,
-            precision=PREC_FP64, evals_cap=0, steps_cap=0, tpb=0, min_ctas_per_sm=0, stage_obs=0) -> FitResult:
+            precision=PREC_FP64, evals_cap=0, steps_cap=0, tpb=0, min_ctas_per_sm=0, stage_obs=0,
+            fp64_result=False) -> FitResult:
         """setup_kernel + chi2_gpu + result copies for one pass (asteroid.c:626-759)."""
         self.fit_begin(n_chains, group_size, n_stages, seed, reopt, params0, precision, evals_cap, steps_cap, tpb,
-                       min_ctas_per_sm, stage_obs)
+                       min_ctas_per_sm, stage_obs, fp64_result)
         while not self.fit_step(0):
             pass
         return self.fit_end()
@@ -341,7 +344,7 @@ def probe_peak(kind: str = "fp64", device: int = -1) -> float:
 
 
 def fit_cfg(n_chains=1024, group_size=256, seed=1, reopt=False, params0=None, precision=PREC_FP64, evals_cap=0,
-            steps_cap=0, n_stages=1, tpb=0):
+            steps_cap=0, n_stages=1, tpb=0, fp64_result=False):
     """An ast_fit_cfg; the returned tuple keeps params0 alive while the struct is in use."""
     cfg = capi.FitCfg()
     cfg.seed = int(seed) & ((1 << 64) - 1)
@@ -353,6 +356,7 @@ def fit_cfg(n_chains=1024, group_size=256, seed=1, reopt=False, params0=None, pr
     cfg.evals_cap = int(evals_cap)
     cfg.steps_cap = int(steps_cap)
     cfg.tpb = int(tpb)
+    cfg.fp64_result = int(bool(fp64_result))
     keep = None
     if reopt:
         keep = np.ascontiguousarray(params0, dtype=np.float64)

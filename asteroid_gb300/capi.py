@@ -97,6 +97,7 @@ class FitCfg(C.Structure):
         ("params0", C.POINTER(C.c_double)),
         ("min_ctas_per_sm", C.c_int32),
         ("stage_obs", C.c_int32),
+        ("fp64_result", C.c_int32),
     ]
 
 

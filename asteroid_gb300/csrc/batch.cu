@@ -47,7 +47,7 @@ struct BatchObj {
     const void* obs;
     ObsLayout L;
     int64_t chain0, n_chains;
-    int32_t group_size, reopt, steps_cap, pad;
+    int32_t group_size, reopt, steps_cap, fp64_result;
     uint64_t seed;
     int64_t evals_cap;
     CF* x_start;               // [G][N] start points under reopt, else unused
@@ -187,7 +187,8 @@ __global__ void batch_group_best_kernel(const BatchObj<CF>* objs, const int2* gm
 {
     const int2 kg = gmap[blockIdx.x];
     const BatchObj<CF>& B = objs[kg.x];
-    group_best_body<CF>(B.M, obj_view(V, B), kg.y, B.out_f, B.out_p, B.out_dv);
+    const ObsView o = B.L.view(B.obs, B.M.n_data);
+    group_best_body<CF>(B.M, obj_view(V, B), kg.y, B.out_f, B.out_p, B.out_dv, B.fp64_result ? &o : nullptr);
 }
 
 __global__ void batch_reset_kernel(int64_t* chain, int32_t* st, int32_t* it, int32_t* ev, int64_t S)
@@ -219,7 +220,7 @@ struct Entry {
     ObsLayout L{};
     int32_t N = 0, NF = 0;
     int64_t n_chains = 0, groups = 0;
-    int32_t group_size = 0, reopt = 0, steps_cap = 0;
+    int32_t group_size = 0, reopt = 0, steps_cap = 0, fp64_result = 0;
     uint64_t seed = 0;
     int64_t evals_cap = 0;
     std::vector<unsigned char> img;  // host image of the observation block
@@ -396,6 +397,7 @@ static int pool_new_entry(ast_pool& P, const ast_model* model, const ast_obs_set
     e->groups = cfg->n_chains / cfg->group_size;
     e->reopt = cfg->reopt ? 1 : 0;
     e->steps_cap = cfg->steps_cap > 0 ? cfg->steps_cap : 5000;
+    e->fp64_result = (cfg->precision == AST_PREC_MIXED && cfg->fp64_result) ? 1 : 0;
     e->seed = cfg->seed;
     e->evals_cap = cfg->evals_cap;
     e->L = ObsLayout::make(obs->n_data);
@@ -467,6 +469,7 @@ static BatchObj<CF> make_obj(const ast_pool& P, const Entry* e)
     o.group_size = e->group_size;
     o.reopt = e->reopt;
     o.steps_cap = e->steps_cap;
+    o.fp64_result = e->fp64_result;
     o.seed = e->seed;
     o.evals_cap = e->evals_cap;
     o.x_start = (CF*)(b + e->off_xs);

@@ -99,9 +99,11 @@ __global__ void __launch_bounds__(256, MINB) fit_kernel(DevModel M, const void* 
 // Per-group argmin over the chains' results (lowest chi^2, lowest chain on ties, as the serial
 // loop of cuda.c:1770-1782) and the stage hand-off or the final output (cuda.c:1785-1823).
 template <class CF>
-__global__ void group_best_kernel(DevModel M, FitView<CF> V, double* out_f, double* out_p, double* out_dv)
+__global__ void group_best_kernel(DevModel M, FitView<CF> V, double* out_f, double* out_p, double* out_dv,
+                                  const void* g_obs, ObsLayout L, int fp64_result)
 {
-    group_best_body<CF>(M, V, blockIdx.x, out_f, out_p, out_dv);
+    const ObsView o = L.view(g_obs, M.n_data);
+    group_best_body<CF>(M, V, blockIdx.x, out_f, out_p, out_dv, fp64_result ? &o : nullptr);
 }
 
 __global__ void reset_slots_kernel(int64_t* chain, int32_t* st, int32_t* it, int32_t* ev, double* dv, int64_t S, int NF)
@@ -319,7 +321,9 @@ static int fit_step_t(ast_ctx* c, int64_t budget, int32_t* done, cudaStream_t s)
         return AST_OK;
     }
     // Stage finished: group argmin, hand-off or output.
-    group_best_kernel<CF><<<(unsigned)b.groups, 256, 0, s>>>(c->dm, V, b.out_f, b.out_p, b.out_dv);
+    const int fp64_result = (PREC == AST_PREC_MIXED && r.cfg.fp64_result) ? 1 : 0;
+    group_best_kernel<CF><<<(unsigned)b.groups, 256, 0, s>>>(c->dm, V, b.out_f, b.out_p, b.out_dv, c->d_obs,
+                                                               c->layout, fp64_result);
     AST_CUDA(cudaGetLastError());
     if (r.stage == r.cfg.n_stages - 1) {
         *done = 1;
@@ -540,7 +544,7 @@ static int noalloc_run(const DevModel& dm, char* base, const int64_t* off, const
         if (h[1] != (unsigned long long)C)
             return ast_set_error(AST_E_TIMEOUT, "ast_fit_noalloc: stage %d finished %llu of %lld chains", stage, h[1],
                                  (long long)C);
-        group_best_kernel<CF><<<(unsigned)G, 256, 0, s>>>(dm, V, d_best_f, d_best_params, d_best_dv);
+        group_best_kernel<CF><<<(unsigned)G, 256, 0, s>>>(dm, V, d_best_f, d_best_params, d_best_dv, nullptr, L, 0);
         AST_CUDA(cudaGetLastError());
         V.reopt = 1;
         unsigned long long z[2] = {0, 0};

@@ -317,10 +317,11 @@ __device__ __forceinline__ bool slot_iterate(const DevModel& M, const ObsView& o
 
 // Argmin over group g of V's chains (lowest chi^2, lowest chain on ties, as the serial loop of
 // cuda.c:1770-1782) and the stage hand-off or the final output (cuda.c:1785-1823).  One CTA per
-// group.
+// group.  With fp64_obs (a mixed-precision fit asked for FP64 results), the reported chi^2 of the
+// group is the plain FP64 path's chi^2 at its best parameters.
 template <class CF>
 __device__ void group_best_body(const DevModel& M, const FitView<CF>& V, int64_t g, double* out_f, double* out_p,
-                                double* out_dv)
+                                double* out_dv, const ObsView* fp64_obs = nullptr)
 {
     const int N = M.n_params, NF = M.n_filters;
     double best = kHuge;
@@ -359,6 +360,10 @@ __device__ void group_best_body(const DevModel& M, const FitView<CF>& V, int64_t
         double p[AST_MAX_PARAMS];
         for (int i = 0; i < N; i++) p[i] = 0;
         if (best < kHuge) x2params<CF>(M, V.reopt, xb, p);
+        if (fp64_obs && best < kHuge) {
+            double d[AST_MAX_FILTERS];
+            out_f[g] = (double)chi2_fp64<double>(M, *fp64_obs, p, d);
+        }
         for (int i = 0; i < N; i++) out_p[g * N + i] = p[i];
         for (int m = 0; m < NF; m++) out_dv[g * NF + m] = best < kHuge ? V.chain_dv[cb * NF + m] : 0.0;
     }

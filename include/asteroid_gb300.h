@@ -231,6 +231,9 @@ typedef struct ast_fit_cfg {
     int32_t  min_ctas_per_sm; /* register budget: 1 (or 0) = up to 255 registers/thread, 2 = 128 */
     int32_t  stage_obs;     /* observations in shared memory: 1 = always when they fit, -1 = never,
                                  0 = only when it does not lower the CTAs per SM */
+    int32_t  fp64_result;   /* AST_PREC_MIXED only: report each group's chi^2 as the plain FP64
+                                 path's chi^2 at its best parameters (one FP64 evaluation per group
+                                 at the end); the search itself stays mixed.  0 = the mixed chi^2 */
 } ast_fit_cfg;
 
 typedef struct ast_fit_out {

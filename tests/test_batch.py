@@ -117,3 +117,25 @@ def test_server_admits_by_hbm_budget(gpu, synth_objects):
             assert st["hbm_used"] <= st["hbm_budget"] and running <= 1
         for k, i in enumerate(ids):
             same(srv.poll(i)[0], single(s, api.PREC_FP64, 5 + k))
+
+
+def test_fp64_results_of_a_mixed_fit(gpu, synth_objects):
+    """fp64_result: each group's reported chi^2 is the plain path's chi^2 at the group's best
+    parameters, the same alone (ast_fit) and in a batch, and the search stays the mixed one."""
+    objs = [synth_objects(n) for n in ("c3_0", "c3_2")]
+    with api.Batch(precision=api.PREC_MIXED, acc=True, n_slots=152 * 32) as b:
+        for k, s in enumerate(objs):
+            b.add(s.model, s.obs, **dict(CFG, seed=40 + k), fp64_result=True)
+        b.run()
+        got = [b.result(i) for i in range(len(objs))]
+    for k, s in enumerate(objs):
+        with api.Engine(s.model, s.obs) as eng:
+            plain = eng.fit(n_chains=CFG["n_chains"], group_size=CFG["group_size"], seed=40 + k,
+                            evals_cap=CFG["evals_cap"], precision=api.PREC_MIXED)
+            pol = eng.fit(n_chains=CFG["n_chains"], group_size=CFG["group_size"], seed=40 + k,
+                          evals_cap=CFG["evals_cap"], precision=api.PREC_MIXED, fp64_result=True)
+            c64, _ = eng.eval(pol.best_params, api.PREC_FP64)
+        same(got[k], pol)
+        assert np.array_equal(pol.best_params, plain.best_params)  # same search
+        ok = pol.best_f < 1e29
+        assert ok.any() and np.allclose(pol.best_f[ok], c64[ok], rtol=1e-12, atol=0)
