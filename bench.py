@@ -47,7 +47,7 @@ UNIT = "evals/s"
 # of one launch over 38 912 slots (the slot state in and out; independent of the evaluations per
 # slot).  Other workloads scale the per-evaluation figures by their RK4 step count.
 NCU_C2 = {"rk4_steps": 12568, "mixed_fp32_flops": 3.497e7, "fp64_flops": 7.75e6,
-          "slots": 38912, "dram_bytes_mixed": 1.084e8, "dram_bytes_fp64": 7.91e7}
+          "slots": 38912, "dram_bytes_mixed": 9.97e7, "dram_bytes_fp64": 5.71e6}
 
 
 def rk4_steps(obs, time_step):
