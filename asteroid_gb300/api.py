@@ -443,12 +443,14 @@ class Batch:
 class Server:
     """Continuous batching of fit requests (ast_server_*, ast_submit, ast_poll)."""
 
-    def __init__(self, precision=PREC_MIXED, acc=True, n_slots=0, hbm_budget=0, device=-1):
+    def __init__(self, precision=PREC_MIXED, acc=True, n_slots=0, hbm_budget=0, device=-1, lanes=1):
         self.lib = capi.load()
         h = C.c_void_p()
         check(self.lib.ast_server_create(int(device), int(precision), int(bool(acc)), int(n_slots), int(hbm_budget),
                                          C.byref(h)), "ast_server_create")
         self.h = h
+        if lanes != 1:
+            check(self.lib.ast_server_set_lanes(self.h, int(lanes)), "ast_server_set_lanes")
         self.precision = precision
         self.items = {}
 

@@ -171,6 +171,7 @@ SIGNATURES = {
                                      C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "ast_batch_destroy": (None, [_P]),
     "ast_server_create": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int64, C.c_int64, C.POINTER(_P)]),
+    "ast_server_set_lanes": (C.c_int, [_P, C.c_int32]),
     "ast_submit": (C.c_int, [_P, C.POINTER(Model), C.POINTER(ObsSet), C.POINTER(FitCfg), C.POINTER(C.c_int64)]),
     "ast_server_step": (C.c_int, [_P, C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "ast_poll": (C.c_int, [_P, C.c_int64, C.POINTER(FitOut), C.POINTER(C.c_double)]),

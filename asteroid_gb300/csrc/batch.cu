@@ -181,6 +181,251 @@ __global__ void __launch_bounds__(256, 1) batch_kernel(const BatchObj<CF>* objs,
     if (n_fit) atomicAdd(&V.ctr[3], n_fit);
 }
 
+// ---------------------------------------------------------------- cooperative chains
+//
+// For a lightly loaded server (few chains in flight, each 5000 sequential evaluations), a chain
+// can use G lanes instead of one.  Each round the group's leader lane lists the points the
+// sequential chain may evaluate next -- the N+1 start vertices (G at a time), the reflection,
+// expansion and inside contraction of an iteration (all three at once), the shrunk vertices (G
+// at a time) -- the G lanes evaluate them side by side, and the leader applies the results in
+// the sequential order, counting only the evaluations the one-lane chain makes.  The chain's
+// path, counters and result are those of slot_iterate, bit for bit; an iteration costs one
+// round instead of one to two evaluations in a row, and INIT and SHRINK G times fewer.
+
+constexpr int kCoopLanes = 4;
+
+// The slot-buffer accessors of simplex.cuh (vertex v's coordinate i, its value, the sort index,
+// the centroid, the trial point), for slot s of a view V with stride S and N parameters.
+#define XV(v, i) V.x[((int64_t)(v) * N + (i)) * S + s]
+#define FV(v) V.f[(int64_t)(v) * S + s]
+#define IND(v) V.ind[(int64_t)(v) * S + s]
+#define X0V(i) V.x0[(int64_t)(i) * S + s]
+#define XRV(i) V.xr[(int64_t)(i) * S + s]
+
+template <class CF>
+struct CoopXchg {  // one group's exchange area in shared memory
+    CF pts[kCoopLanes][AST_MAX_PARAMS];
+    CF f[kCoopLanes];
+    CF dv[kCoopLanes][AST_MAX_FILTERS];
+    int32_t rej[kCoopLanes];
+    int32_t dv_set[kCoopLanes];
+};
+
+// The points of the next round into X; returns how many.
+template <class CF>
+__device__ int coop_plan(const DevModel& M, const FitView<CF>& V, int64_t s, const SlotState<CF>& R, CoopXchg<CF>& X)
+{
+    const int N = M.n_params;
+    const int64_t S = V.S;
+    const int phase = R.st & 0xff, j = (R.st >> 8) & 0xff;
+    if (phase == PH_REFLECT) {
+        const int w = IND(N);
+        for (int i = 0; i < N; i++) {
+            const CF c0 = X0V(i), xr = XRV(i);
+            X.pts[0][i] = xr;
+            X.pts[1][i] = (M.frozen[i] != 1) ? c0 + (CF)2.0 * (xr - c0) : c0;         // expansion
+            X.pts[2][i] = (M.frozen[i] != 1) ? c0 + (CF)0.5 * (XV(w, i) - c0) : c0;   // contraction
+        }
+        return 3;
+    }
+    const int n = min(kCoopLanes, N + 1 - j);
+    for (int k = 0; k < n; k++) {
+        const int v = phase == PH_INIT ? j + k : IND(j + k);
+        for (int i = 0; i < N; i++) X.pts[k][i] = XV(v, i);
+    }
+    return n;
+}
+
+// The round's results in the sequential order (cuda.c:1546-1742): returns true when the chain
+// ends; *failed as slot_iterate.
+template <class CF>
+__device__ bool coop_apply(const DevModel& M, const FitView<CF>& V, int64_t s, SlotState<CF>& R, const CoopXchg<CF>& X,
+                           int n, unsigned long long& n_ev, bool* failed)
+{
+    const int N = M.n_params, NF = M.n_filters;
+    const int64_t S = V.S;
+    const CF HUGEV = (CF)kHuge;
+    int32_t st = R.st;
+    const int phase = st & 0xff;
+    int j = (st >> 8) & 0xff;
+    int bad = (st >> 16) & 1;
+    *failed = false;
+    // An evaluation the one-lane chain makes: counted, and its delta_V kept when it wrote one.
+    auto use = [&](int k) -> CF {
+        R.ev++;
+        n_ev++;
+        if (X.dv_set[k])
+            for (int m = 0; m < NF; m++) R.dvl[m] = X.dv[k][m];
+        return X.f[k];
+    };
+    bool iter_top = false;
+    if (phase == PH_INIT) {
+        for (int k = 0; k < n; k++) {
+            if (X.rej[k]) {
+                *failed = true;
+                return true;
+            }
+            FV(j) = use(k);
+            j++;
+        }
+        if (j > N) iter_top = true;
+        else st = PH_INIT | (j << 8);
+    } else if (phase == PH_REFLECT) {
+        const CF f_r = X.rej[0] ? HUGEV : use(0);
+        const int b = IND(0), sw = IND(N - 1), w = IND(N);
+        if (f_r >= FV(b) && f_r < FV(sw)) {
+            for (int i = 0; i < N; i++) XV(w, i) = X.pts[0][i];
+            FV(w) = f_r;
+        } else if (f_r < FV(b)) {
+            const CF f_e = X.rej[1] ? HUGEV : use(1);
+            const int from = f_e < f_r ? 1 : 0;
+            for (int i = 0; i < N; i++) XV(w, i) = X.pts[from][i];
+            FV(w) = from ? f_e : f_r;
+        } else {
+            for (int i = 0; i < N; i++) XRV(i) = X.pts[2][i];
+            const CF f_c = X.rej[2] ? HUGEV : use(2);
+            if (f_c < FV(w)) {
+                for (int i = 0; i < N; i++) XV(w, i) = X.pts[2][i];
+                FV(w) = f_c;
+            } else {
+                // Shrink every vertex but the best towards it (cuda.c:1716-1727); the best does
+                // not move, so all of them can be shrunk before they are evaluated.
+                for (int jj = 1; jj <= N; jj++) {
+                    const int v = IND(jj);
+                    for (int i = 0; i < N; i++)
+                        if (M.frozen[i] != 1) XV(v, i) = XV(b, i) + (CF)0.5 * (XV(v, i) - XV(b, i));
+                }
+                R.st = PH_SHRINK | (1 << 8);
+                return false;
+            }
+        }
+        iter_top = true;
+    } else {  // PH_SHRINK
+        for (int k = 0; k < n; k++, j++) {
+            if (X.rej[k]) bad = 1;
+            else FV(IND(j)) = use(k);
+        }
+        if (j <= N) {
+            st = PH_SHRINK | (j << 8) | (bad << 16);
+        } else if (bad) {
+            *failed = true;
+            return true;
+        } else {
+            iter_top = true;
+        }
+    }
+    bool finish = false;
+    if (iter_top && nm_iter_top<CF>(M, V, s, R, st)) finish = true;
+    R.st = st;
+    return finish;
+}
+
+#undef XV
+#undef FV
+#undef IND
+#undef X0V
+#undef XRV
+
+// G = kCoopLanes lanes per slot; V.n_slots counts groups.  Dynamic shared memory: one CoopXchg
+// per group.
+template <class CF, int PREC>
+__global__ void __launch_bounds__(256, 1) coop_kernel(const BatchObj<CF>* objs, int n_objs, FitView<CF> V,
+                                                      int64_t budget)
+{
+    constexpr int G = kCoopLanes;
+    __shared__ float4 trig[PREC == AST_PREC_MIXED ? kTrigTable : 1];
+    extern __shared__ __align__(16) unsigned char coop_smem[];
+    if (PREC == AST_PREC_MIXED) {
+        trig_table_fill(trig);
+        __syncthreads();
+    }
+    const int r = threadIdx.x % G;
+    const int64_t s = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / G;
+    if (s >= V.n_slots) return;  // whole groups leave
+    CoopXchg<CF>& X = ((CoopXchg<CF>*)coop_smem)[threadIdx.x / G];
+    const unsigned mask = ((1u << G) - 1u) << ((threadIdx.x & 31u) & ~(unsigned)(G - 1));
+    const int leader = (int)((threadIdx.x & 31u) & ~(unsigned)(G - 1));
+    const int64_t S = V.S;
+    int64_t gchain = -1;
+    int k = 0;
+    SlotState<CF> R;
+    R.chain = -1;
+    unsigned long long n_ev = 0, n_fit = 0, n_done = 0;
+    if (r == 0) {
+        gchain = V.chain[s];
+        R.st = V.st[s];
+        R.l = V.it[s];
+        R.ev = V.ev[s];
+        for (int m = 0; m < AST_MAX_FILTERS; m++) R.dvl[m] = (CF)0;
+        if (gchain >= 0) {
+            k = find_obj(objs, n_objs, gchain);
+            R.chain = gchain - objs[k].chain0;
+            for (int m = 0; m < objs[k].M.n_filters; m++) R.dvl[m] = (CF)V.dv[(int64_t)m * S + s];
+        }
+    }
+    for (int64_t used = 0; used < budget; used++) {
+        int n = 0, stop = 0;
+        if (r == 0) {
+            if (gchain < 0) {
+                const unsigned long long c = atomicAdd(&V.ctr[0], 1ull);
+                if (c >= (unsigned long long)V.n_chains) stop = 1;
+                else {
+                    gchain = (int64_t)c;
+                    batch_start<CF>(objs, n_objs, V, s, gchain, k, R);
+                }
+            }
+            if (!stop) n = coop_plan<CF>(objs[k].M, obj_view(V, objs[k]), s, R, X);
+        }
+        stop = __shfl_sync(mask, stop, leader);
+        if (stop) break;
+        n = __shfl_sync(mask, n, leader);
+        const int kk = __shfl_sync(mask, k, leader);
+        __syncwarp(mask);
+        if (r < n) {
+            const BatchObj<CF>& B = objs[kk];
+            const ObsView o = B.L.view(B.obs, B.M.n_data);
+            CF p[AST_MAX_PARAMS];
+            for (int i = 0; i < B.M.n_params; i++) p[i] = X.pts[r][i];
+            double params[AST_MAX_PARAMS];
+            const int rej = x2params<CF>(B.M, B.reopt, p, params);
+            const CF unset = (CF)-7.5e37f;  // no chi^2 writes this delta_V: tells an early exit apart
+            CF dvl[AST_MAX_FILTERS];
+            for (int m = 0; m < AST_MAX_FILTERS; m++) dvl[m] = unset;
+            CF fv = (CF)kHuge;
+            if (!rej) fv = eval_point<CF, PREC>(B.M, o, params, dvl, trig);
+            X.f[r] = fv;
+            X.rej[r] = rej;
+            X.dv_set[r] = !rej && dvl[0] != unset;
+            for (int m = 0; m < AST_MAX_FILTERS; m++) X.dv[r][m] = dvl[m];
+        }
+        __syncwarp(mask);
+        if (r == 0) {
+            const BatchObj<CF>& B = objs[k];
+            const FitView<CF> W = obj_view(V, B);
+            bool failed = false;
+            if (coop_apply<CF>(B.M, W, s, R, X, n, n_ev, &failed)) {
+                nm_finish<CF>(B.M, W, s, R, failed, n_fit);
+                atomicAdd(B.done, 1ull);
+                n_done++;
+                gchain = -1;
+                R.chain = -1;
+            }
+        }
+        __syncwarp(mask);
+    }
+    if (r == 0) {
+        V.chain[s] = gchain;
+        V.st[s] = R.st;
+        V.it[s] = R.l;
+        V.ev[s] = R.ev;
+        if (gchain >= 0)
+            for (int m = 0; m < objs[k].M.n_filters; m++) V.dv[(int64_t)m * S + s] = (double)R.dvl[m];
+        if (n_done) atomicAdd(&V.ctr[1], n_done);
+        if (n_ev) atomicAdd(&V.ctr[2], n_ev);
+        if (n_fit) atomicAdd(&V.ctr[3], n_fit);
+    }
+}
+
 // One CTA per (object, group) of gmap.
 template <class CF>
 __global__ void batch_group_best_kernel(const BatchObj<CF>* objs, const int2* gmap, FitView<CF> V)
@@ -276,6 +521,8 @@ struct ast_pool {
     std::vector<int> free_done;
     // launch geometry
     int tpb = 256, refill = 1, ctas = 0;
+    int lanes = 1;      // lanes per chain: 1, or kCoopLanes (cooperative chains, servers only)
+    size_t smem = 0;    // dynamic shared memory of the launch
     // entries
     std::vector<Entry*> all;                    // by id
     std::vector<Entry*> active;                 // running, by chain0
@@ -505,7 +752,7 @@ static FitView<CF> pool_view(const ast_pool& P)
     V.x = (CF*)P.x; V.f = (CF*)P.f; V.ind = P.ind; V.x0 = (CF*)P.x0; V.xr = (CF*)P.xr; V.fr = (CF*)P.fr;
     V.st = P.st; V.it = P.it; V.ev = P.ev; V.chain = P.chain; V.dv = P.dv; V.ctr = P.ctr;
     V.S = P.S;
-    V.n_slots = (int64_t)P.ctas * P.tpb;
+    V.n_slots = (int64_t)P.ctas * P.tpb / P.lanes;
     V.n_chains = P.chain_end;
     V.last_stage = 1;
     return V;
@@ -517,10 +764,31 @@ static decltype(&batch_kernel<CF, PREC, 1>) batch_kernel_ptr(int refill)
     return refill == 32 ? batch_kernel<CF, PREC, 32> : batch_kernel<CF, PREC, 1>;
 }
 
+// Cooperative chains: CTA size -> CTAs (full occupancy, groups capped by the slot pool).
+template <class CF, int PREC>
+static int coop_geometry(ast_pool& P, int tpb)
+{
+    const size_t smem = (size_t)(tpb / kCoopLanes) * sizeof(CoopXchg<CF>);
+    auto kern = coop_kernel<CF, PREC>;
+    if (smem > 48 * 1024) AST_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int occ = 0;
+    AST_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, tpb, smem));
+    if (occ < 1) return ast_set_error(AST_E_TOO_LARGE, "server: cooperative kernel does not fit on an SM");
+    int64_t ctas = (int64_t)P.sm_count * occ;
+    if (ctas * tpb > P.n_slots * kCoopLanes) ctas = P.n_slots * kCoopLanes / tpb;
+    if (ctas < 1) return ast_set_error(AST_E_INVALID, "server: slot pool smaller than one CTA");
+    P.tpb = tpb;
+    P.refill = 1;
+    P.ctas = (int)ctas;
+    P.smem = smem;
+    return AST_OK;
+}
+
 // CTA size and refill mapping -> CTAs (full occupancy, capped by the slot pool).
 template <class CF, int PREC>
 static int pool_geometry(ast_pool& P, int tpb, int refill)
 {
+    if (P.lanes > 1) return coop_geometry<CF, PREC>(P, 128);
     if (tpb < 32 || tpb > 256 || (tpb & 31)) return ast_set_error(AST_E_INVALID, "batch: tpb must be 32..256, x32");
     if (refill != 1 && refill != 32) return ast_set_error(AST_E_INVALID, "batch: refill must be 1 or 32");
     int occ = 0;
@@ -847,6 +1115,18 @@ extern "C" int ast_server_create(int32_t device, int32_t precision, int32_t acc,
     return AST_OK;
 }
 
+extern "C" int ast_server_set_lanes(ast_server* V, int32_t lanes_per_chain)
+{
+    if (!V) return ast_set_error(AST_E_INVALID, "ast_server_set_lanes: NULL server");
+    if (lanes_per_chain != 1 && lanes_per_chain != kCoopLanes)
+        return ast_set_error(AST_E_INVALID, "ast_server_set_lanes: lanes per chain must be 1 or %d", kCoopLanes);
+    if (!V->P.active.empty() || V->P.evals)
+        return ast_set_error(AST_E_INVALID, "ast_server_set_lanes: the server has already run requests");
+    V->P.lanes = lanes_per_chain;
+    V->P.ctas = 0;  // the geometry is chosen again at the next step
+    return AST_OK;
+}
+
 extern "C" int ast_submit(ast_server* V, const ast_model* model, const ast_obs_set* obs, const ast_fit_cfg* cfg,
                           int64_t* request)
 {
@@ -879,8 +1159,12 @@ static int server_step_t(ast_server* V, int64_t evals_per_slot, int32_t* n_runni
         if ((rc = upload_table<CF>(P))) return rc;
         const FitView<CF> W = pool_view<CF>(P);
         AST_CUDA(cudaEventRecord(P.ev0, P.stream));
-        batch_kernel_ptr<CF, PREC>(P.refill)<<<P.ctas, P.tpb, 0, P.stream>>>(
-            (const BatchObj<CF>*)P.d_objs, (int)P.active.size(), W, evals_per_slot);
+        if (P.lanes > 1)
+            coop_kernel<CF, PREC><<<P.ctas, P.tpb, P.smem, P.stream>>>((const BatchObj<CF>*)P.d_objs,
+                                                                       (int)P.active.size(), W, evals_per_slot);
+        else
+            batch_kernel_ptr<CF, PREC>(P.refill)<<<P.ctas, P.tpb, 0, P.stream>>>(
+                (const BatchObj<CF>*)P.d_objs, (int)P.active.size(), W, evals_per_slot);
         AST_CUDA(cudaGetLastError());
         AST_CUDA(cudaEventRecord(P.ev1, P.stream));
         unsigned long long h[8];

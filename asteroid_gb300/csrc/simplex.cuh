@@ -147,6 +147,82 @@ struct SlotState {
     CF dvl[AST_MAX_FILTERS];
 };
 
+// End of a simplex iteration (cuda.c:1575-1640): selection sort with ties to the last index
+// (an all-NaN simplex keeps ind[0] = 0 with f = 1e30), centroid of all N+1 vertices, the size,
+// iteration and evaluation caps, and the next reflection point.  Returns true if the chain ends.
+template <class CF>
+__device__ __forceinline__ bool nm_iter_top(const DevModel& M, const FitView<CF>& V, int64_t s, SlotState<CF>& R,
+                                            int32_t& st)
+{
+    const int N = M.n_params;
+    const int64_t S = V.S;
+    const CF HUGEV = (CF)kHuge;
+    const CF size2_min = NMConst<CF>::size2_min();
+    bool finish = false;
+    R.l++;
+    // Selection sort, ties to the last index; an all-NaN simplex keeps ind[0] = 0
+    // with f = 1e30 (cuda.c:1575-1601).
+    uint32_t taken = 0;
+    for (int jj = 0; jj <= N; jj++) {
+        CF fmin = HUGEV;
+        int jmin = -1;
+        for (int j2 = 0; j2 <= N; j2++) {
+            const CF fj = FV(j2);
+            if (!(taken >> j2 & 1u) && fj <= fmin) { fmin = fj; jmin = j2; }
+        }
+        if (jmin < 0) {
+            IND(0) = 0;
+            FV(0) = HUGEV;
+            break;
+        }
+        IND(jj) = (uint8_t)jmin;
+        taken |= 1u << jmin;
+    }
+    // Centroid of all N+1 vertices and the size test (cuda.c:1604-1632).
+    CF size2 = 0;
+    for (int i = 0; i < N; i++) {
+        CF sum = 0;
+        for (int v = 0; v <= N; v++) sum = sum + XV(v, i);
+        X0V(i) = sum / (CF)(N + 1);
+    }
+    for (int v = 0; v <= N; v++) {
+        CF sum = 0;
+        for (int i = 0; i < N; i++) {
+            const CF dx = XV(v, i) - X0V(i);
+            sum = sum + dx * dx;
+        }
+        size2 = size2 + sum;
+    }
+    size2 = size2 / (CF)N;
+    if (size2 < size2_min || R.l > V.steps_cap || (V.evals_cap > 0 && R.ev >= V.evals_cap)) {
+        finish = true;
+    } else {
+        const int w = IND(N);
+        for (int i = 0; i < N; i++) {
+            const CF c0 = X0V(i);
+            XRV(i) = (M.frozen[i] != 1) ? c0 + (CF)1.0 * (c0 - XV(w, i)) : c0;
+        }
+        st = PH_REFLECT;
+    }
+    return finish;
+}
+
+// A finished chain's result: its best vertex and value (vertex 0 and 1e30 if it failed) and the
+// delta_V of its last evaluation (cuda.c:1760-1821).
+template <class CF>
+__device__ __forceinline__ void nm_finish(const DevModel& M, const FitView<CF>& V, int64_t s, const SlotState<CF>& R,
+                                          bool failed, unsigned long long& n_fit)
+{
+    const int N = M.n_params, NF = M.n_filters;
+    const int64_t S = V.S;
+    const int64_t chain = R.chain;
+    const int b = failed ? 0 : IND(0);
+    V.chain_f[chain] = failed ? kHuge : (double)FV(b);
+    for (int i = 0; i < N; i++) V.chain_x[chain * N + i] = XV(b, i);
+    for (int m = 0; m < NF; m++) V.chain_dv[chain * NF + m] = (double)R.dvl[m];
+    n_fit += V.last_stage ? 1 : 0;
+}
+
 // One evaluation of the slot's chain and the simplex move it completes (cuda.c:1546-1760),
 // as a state machine: INIT evaluates the N+1 start vertices, then REFLECT / EXPAND / CONTRACT /
 // SHRINK.  V carries the slot buffers and the chain-level settings of the chain's object.
@@ -156,10 +232,9 @@ __device__ __forceinline__ bool slot_iterate(const DevModel& M, const ObsView& o
                                              SlotState<CF>& R, const float4* trig, unsigned long long& n_ev,
                                              unsigned long long& n_fit)
 {
-    const int N = M.n_params, NF = M.n_filters;
+    const int N = M.n_params;
     const int64_t S = V.S;
     const CF HUGEV = (CF)kHuge;
-    const CF size2_min = NMConst<CF>::size2_min();
     int32_t st = R.st;
     const int phase = st & 0xff;
     int j = (st >> 8) & 0xff;
@@ -255,62 +330,9 @@ __device__ __forceinline__ bool slot_iterate(const DevModel& M, const ObsView& o
             iter_top = true;
         }
     }
-    if (iter_top) {
-        R.l++;
-        // Selection sort, ties to the last index; an all-NaN simplex keeps ind[0] = 0
-        // with f = 1e30 (cuda.c:1575-1601).
-        uint32_t taken = 0;
-        for (int jj = 0; jj <= N; jj++) {
-            CF fmin = HUGEV;
-            int jmin = -1;
-            for (int j2 = 0; j2 <= N; j2++) {
-                const CF fj = FV(j2);
-                if (!(taken >> j2 & 1u) && fj <= fmin) { fmin = fj; jmin = j2; }
-            }
-            if (jmin < 0) {
-                IND(0) = 0;
-                FV(0) = HUGEV;
-                break;
-            }
-            IND(jj) = (uint8_t)jmin;
-            taken |= 1u << jmin;
-        }
-        // Centroid of all N+1 vertices and the size test (cuda.c:1604-1632).
-        CF size2 = 0;
-        for (int i = 0; i < N; i++) {
-            CF sum = 0;
-            for (int v = 0; v <= N; v++) sum = sum + XV(v, i);
-            X0V(i) = sum / (CF)(N + 1);
-        }
-        for (int v = 0; v <= N; v++) {
-            CF sum = 0;
-            for (int i = 0; i < N; i++) {
-                const CF dx = XV(v, i) - X0V(i);
-                sum = sum + dx * dx;
-            }
-            size2 = size2 + sum;
-        }
-        size2 = size2 / (CF)N;
-        if (size2 < size2_min || R.l > V.steps_cap || (V.evals_cap > 0 && R.ev >= V.evals_cap)) {
-            finish = true;
-        } else {
-            const int w = IND(N);
-            for (int i = 0; i < N; i++) {
-                const CF c0 = X0V(i);
-                XRV(i) = (M.frozen[i] != 1) ? c0 + (CF)1.0 * (c0 - XV(w, i)) : c0;
-            }
-            st = PH_REFLECT;
-        }
-    }
+    if (iter_top && nm_iter_top<CF>(M, V, s, R, st)) finish = true;
     R.st = st;
-    if (finish) {
-        const int64_t chain = R.chain;
-        const int b = failed ? 0 : IND(0);
-        V.chain_f[chain] = failed ? kHuge : (double)FV(b);
-        for (int i = 0; i < N; i++) V.chain_x[chain * N + i] = XV(b, i);
-        for (int m = 0; m < NF; m++) V.chain_dv[chain * NF + m] = (double)R.dvl[m];
-        n_fit += V.last_stage ? 1 : 0;
-    }
+    if (finish) nm_finish<CF>(M, V, s, R, failed, n_fit);
     return finish;
 }
 

@@ -363,6 +363,7 @@ def bench_serve(args, tmp, rank, world):
     pool = synth.generate_batch(32, tmp)
     rng = np.random.default_rng(2024)
     line = {"metric": "fit_latency", "unit": "s", "mode": "serve", "requests_per_rate": args.requests,
+            "lanes_per_chain": args.lanes,
             "chains_per_request": 1024, "evals_per_chain": 5000, "hbm_budget_gb": 150, "rates": {}}
     checked = []
     engines = {}
@@ -370,7 +371,7 @@ def bench_serve(args, tmp, rank, world):
     alone = []
     for k in range(4):
         s = pool[k]
-        with api.Server(precision=api.PREC_MIXED, acc=True, hbm_budget=150 << 30) as srv:
+        with api.Server(precision=api.PREC_MIXED, acc=True, hbm_budget=150 << 30, lanes=args.lanes) as srv:
             r = srv.submit(s.model, s.obs, n_chains=1024, group_size=256, seed=100 + k, evals_cap=5000,
                                    fp64_result=True)
             while srv.poll(r) is None:
@@ -380,7 +381,7 @@ def bench_serve(args, tmp, rank, world):
     line["alone"] = alone
     for lam in (1.0, 4.0, 16.0, 64.0):
         arrivals = np.cumsum(rng.exponential(1.0 / lam, size=args.requests))
-        with api.Server(precision=api.PREC_MIXED, acc=True, hbm_budget=150 << 30) as srv:
+        with api.Server(precision=api.PREC_MIXED, acc=True, hbm_budget=150 << 30, lanes=args.lanes) as srv:
             t0 = time.perf_counter()
             ids, objs, done, lat = [], [], {}, {}
             k = 0
@@ -455,6 +456,7 @@ def main():
                          "--config in both precisions at one seed")
     ap.add_argument("--objects", type=int, default=512, help="batch mode: objects")
     ap.add_argument("--requests", type=int, default=8, help="serve mode: requests per arrival rate")
+    ap.add_argument("--lanes", type=int, default=1, choices=[1, 4], help="serve mode: lanes per chain")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--profile", action="store_true", help="only the fit launches (for ncu)")

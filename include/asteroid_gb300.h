@@ -351,6 +351,12 @@ typedef struct ast_server ast_server;
 /* hbm_budget_bytes <= 0: 150 GiB. */
 int ast_server_create(int32_t device, int32_t precision, int32_t acc, int64_t n_slots, int64_t hbm_budget_bytes,
                       ast_server** out);
+/* Lanes per chain, 1 (default) or 4, set before the first ast_server_step.  With 4, the lanes
+ * of a chain evaluate the points its next simplex move may need side by side (the reflection,
+ * expansion and contraction of an iteration; the start and shrunk vertices four at a time), and
+ * its leader keeps the sequential order: the same results, about half the sequential rounds per
+ * chain -- lower latency while few requests are in flight, a quarter of the chains per slot. */
+int ast_server_set_lanes(ast_server* server, int32_t lanes_per_chain);
 int ast_submit(ast_server* server, const ast_model* model, const ast_obs_set* obs, const ast_fit_cfg* cfg,
                int64_t* request);
 int ast_server_step(ast_server* server, int64_t evals_per_slot, int32_t* n_running, int32_t* n_queued);

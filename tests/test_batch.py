@@ -139,3 +139,22 @@ def test_fp64_results_of_a_mixed_fit(gpu, synth_objects):
         assert np.array_equal(pol.best_params, plain.best_params)  # same search
         ok = pol.best_f < 1e29
         assert ok.any() and np.allclose(pol.best_f[ok], c64[ok], rtol=1e-12, atol=0)
+
+
+@pytest.mark.parametrize("precision", [api.PREC_FP64, api.PREC_MIXED])
+def test_cooperative_chains_equal_single_fits(gpu, synth_objects, precision):
+    """Four lanes per chain (ast_server_set_lanes) evaluate the candidate points of each simplex
+    move side by side; the chain's path and result are those of the one-lane chain, bit for bit."""
+    objs = [synth_objects(n) for n in ("c3_0", "c3_1", "c0acc")]
+    with api.Server(precision=precision, acc=True, n_slots=152 * 64, lanes=4) as srv:
+        ids = [srv.submit(s.model, s.obs, **dict(CFG, seed=60 + k)) for k, s in enumerate(objs)]
+        while any(srv.poll(i) is None for i in ids):
+            srv.step(8)
+        got = [srv.poll(i)[0] for i in ids]
+        evals = srv.stats()["n_evals"]
+    total = 0
+    for k, s in enumerate(objs):
+        ref = single(s, precision, 60 + k)
+        same(got[k], ref)
+        total += ref.n_evals
+    assert evals == total  # only the evaluations the one-lane chains make are counted
