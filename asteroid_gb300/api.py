@@ -166,6 +166,23 @@ def read_data(lc_path, eph_dir=".", interp: bool = False, minima_path=None, max_
         lib.ast_free_host_data(hd)
 
 
+def plot_grid(lc_path, eph_dir=".", n_plot: int = 20000, interp: bool = False):
+    """The -plot grid (read_data.c:309-370): times relative to hMJD0 and unit E, S vectors
+    [n_plot, 3] from the light curve's last ephemeris window, through the C host."""
+    lib = capi.load()
+    hd = C.POINTER(capi.HostData)()
+    check(lib.ast_read_data(str(lc_path).encode(), str(eph_dir).encode(), int(bool(interp)), 8, C.byref(hd)),
+          "ast_read_data")
+    try:
+        t = np.zeros(n_plot)
+        e = np.zeros((n_plot, 3))
+        s = np.zeros((n_plot, 3))
+        check(lib.ast_plot_grid(hd, int(bool(interp)), int(n_plot), dptr(t), dptr(e), dptr(s)), "ast_plot_grid")
+        return t, e, s
+    finally:
+        lib.ast_free_host_data(hd)
+
+
 def format_result(chi2, dv, params) -> str:
     """One output line in the reference's format (asteroid.c:798-811)."""
     lib = capi.load()
@@ -253,6 +270,18 @@ class Engine:
         p = np.ascontiguousarray(params, dtype=np.float64)
         out = np.zeros(self.obs.n_data)
         check(self.lib.ast_model_curve(self.ctx, dptr(p), dptr(out)), "ast_model_curve")
+        return out
+
+    def model_curve_at(self, params, t, e_unit=None, s_unit=None) -> np.ndarray:
+        """Model magnitudes at increasing times t (relative to hMJD0) with unit E, S [n, 3]
+        (unused under INTERP): the -plot model curve."""
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        t = np.ascontiguousarray(t, dtype=np.float64)
+        e = None if e_unit is None else np.ascontiguousarray(e_unit, dtype=np.float64).reshape(-1, 3)
+        s = None if s_unit is None else np.ascontiguousarray(s_unit, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros(t.size)
+        check(self.lib.ast_model_curve_at(self.ctx, dptr(p), int(t.size), dptr(t), dptr(e) if e is not None else None,
+                                          dptr(s) if s is not None else None, dptr(out)), "ast_model_curve_at")
         return out
 
     def model_angles(self, params, precision: int = PREC_FP64) -> np.ndarray:

@@ -133,6 +133,10 @@ SIGNATURES = {
     "ast_x2params": (C.c_int, [C.POINTER(Model), C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "ast_params2x": (C.c_int, [C.POINTER(Model), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "ast_model_curve": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "ast_model_curve_at": (C.c_int, [_P, C.POINTER(C.c_double), C.c_int32, C.POINTER(C.c_double),
+                                     C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "ast_plot_grid": (C.c_int, [C.POINTER(HostData), C.c_int32, C.c_int32, C.POINTER(C.c_double),
+                                C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "ast_model_angles": (C.c_int, [_P, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "ast_read_data": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int32, C.c_int32, C.POINTER(C.POINTER(HostData))]),
     "ast_read_minima": (C.c_int, [C.c_char_p, C.POINTER(HostData)]),

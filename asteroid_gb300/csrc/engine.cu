@@ -411,6 +411,58 @@ extern "C" int ast_model_curve(ast_ctx* c, const double* params, double* vmod)
     return AST_OK;
 }
 
+extern "C" int ast_model_curve_at(ast_ctx* c, const double* params, int32_t n, const double* t,
+                                  const double* e_unit, const double* s_unit, double* vmod)
+{
+    if (!c || !params || !t || !vmod || n < 2) return ast_set_error(AST_E_INVALID, "ast_model_curve_at: bad argument");
+    const bool interp = (c->model.flags & AST_INTERP) != 0;
+    if (!interp && (!e_unit || !s_unit)) return ast_set_error(AST_E_INVALID, "ast_model_curve_at: E and S needed");
+    for (int32_t i = 1; i < n; i++)
+        if (!(t[i] > t[i - 1])) return ast_set_error(AST_E_INVALID, "ast_model_curve_at: times must increase");
+    int rc = set_device(c->device);
+    if (rc) return rc;
+    // A block of n points with the context's model: magnitudes are not used, one filter.
+    std::vector<float> v((size_t)n, 0.0f), w((size_t)n, 1.0f);
+    std::vector<int32_t> f((size_t)n, 0);
+    ast_obs_set o;
+    memset(&o, 0, sizeof(o));
+    o.n_data = n;
+    o.n_filters = 1;
+    o.mjd = t;
+    o.v = v.data();
+    o.w = w.data();
+    o.filter = f.data();
+    o.e_unit = e_unit;
+    o.s_unit = s_unit;
+    DevModel dm = c->dm;
+    dm.n_data = n;
+    dm.n_filters = 1;
+    dm.flags &= ~AST_NUDGE;
+    const ObsLayout L = ObsLayout::make(n);
+    std::vector<unsigned char> img;
+    obs_image(&c->model, &o, L, img);
+    // Device scratch for this call, freed on every return.
+    struct Scratch {
+        void* blk = nullptr;
+        double* p = nullptr;
+        double* v = nullptr;
+        ~Scratch() { cudaFree(blk); cudaFree(p); cudaFree(v); }
+    } d;
+    if (cudaMalloc(&d.blk, (size_t)L.bytes) != cudaSuccess || cudaMalloc(&d.p, sizeof(double) * AST_MAX_PARAMS) != cudaSuccess ||
+        cudaMalloc(&d.v, sizeof(double) * n) != cudaSuccess) {
+        cudaGetLastError();
+        return ast_set_error(AST_E_NOMEM, "ast_model_curve_at: cudaMalloc failed");
+    }
+    AST_CUDA(cudaMemcpyAsync(d.blk, img.data(), img.size(), cudaMemcpyHostToDevice, c->stream));
+    AST_CUDA(cudaMemcpyAsync(d.p, params, sizeof(double) * c->model.n_params, cudaMemcpyHostToDevice, c->stream));
+    if ((rc = launch_prep(dm, (char*)d.blk, L, n, c->stream))) return rc;
+    model_curve_kernel<<<1, 32, 0, c->stream>>>(dm, d.blk, L, d.p, d.v);
+    AST_CUDA(cudaGetLastError());
+    AST_CUDA(cudaMemcpyAsync(vmod, d.v, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    AST_CUDA(cudaStreamSynchronize(c->stream));
+    return AST_OK;
+}
+
 extern "C" int ast_model_angles(ast_ctx* c, int32_t precision, const double* params, double* angles)
 {
     if (!c || !params || !angles) return ast_set_error(AST_E_INVALID, "ast_model_angles: NULL argument");

@@ -1,9 +1,10 @@
 /*
  * asteroid.c -- command-line driver (host, C), the drop-in for the reference's asteroid
- * binary on its fitting path (asteroid.c:18-831 of the reference).
+ * binary on its fitting path (asteroid.c:18-831 of the reference) and its -plot mode
+ * (asteroid.c:834-1060).
  *
  * Same switches and meanings: -i -o -m -t -reopt -keep -best -seed -N -Nstages -f -l -Ppsi
- * (asteroid.c:173-431), same output line ("%13.6e " chi^2, "%13.6e " per-filter delta_V,
+ * -plot (asteroid.c:173-431), same output line ("%13.6e " chi^2, "%13.6e " per-filter delta_V,
  * "%15.11f " parameters in Property order, asteroid.c:798-811), same stdout best line
  * (asteroid.c:770-779), same keep/best/travel semantics (asteroid.c:741-818).  Periodic
  * parameters are printed unwrapped, as the reference does (its wrap loop never runs, see
@@ -14,7 +15,9 @@
  * -DBSIZE, -DTIME_STEP) give the defaults and these extra switches override them at run time:
  *   -variant TORQUE,P_PSI,...   -Nblocks n   -bsize n   -time_step h   -mixed   -evals n
  *   -eph dir (directory of asteroid.eph / earth.eph / sun.eph, default ".")
+ *   -Nplot n (points of the -plot model curve, default NPLOT = 20000)
  */
+#include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -90,11 +93,84 @@ static void usage(void)
     printf("-N number : exit after \"number\" cycles\n");
     printf("-Nstages number : each initial optimization stage is followed by \"number-1\" reoptimization stages\n");
     printf("-o name : output (results) file name\n");
+    printf("-plot : plotting (only makes sense when -m is also used)\n");
     printf("-Ppsi min max : minimum and maximum values for Ppsi period, in hours\n");
     printf("-reopt : reoptimize the model provided with -m switch\n");
     printf("-seed SEED : use the SEED number to initialize the random number generator\n");
     printf("-t : travelling reoptimization\n");
-    printf("\n GB300 engine switches: -variant TORQUE,P_PSI,... -Nblocks n -bsize n -time_step h -mixed -evals n -eph dir\n\n");
+    printf("\n GB300 engine switches: -variant TORQUE,P_PSI,... -Nblocks n -bsize n -time_step h -mixed -evals n -eph dir -Nplot n\n\n");
+}
+
+/* -plot mode (asteroid.c:834-1060, the default build): the chi^2 and delta_V of the -m model on
+ * the data, the model curve on an evenly spaced grid of n_plot times shifted by delta_V of the
+ * first filter, and the files delta_V, model_params.dat, model.dat and data.dat in the
+ * reference's formats.  The model curve is the brightness model alone: NUDGE bookkeeping,
+ * which in the reference can end the curve early after M_MAX minima, plays no part. */
+static int run_plot(const ast_model* m, const ast_host_data* hd, ast_ctx* ctx, const double* params, int interp,
+                    int n_plot)
+{
+    printf("\n*** Plotting ***\n\n");
+    const int N = m->n_params, NF = hd->obs.n_filters;
+    double chi2 = 0, dv[AST_MAX_FILTERS];
+    if (ast_eval_batch(ctx, AST_PREC_FP64, params, 1, &chi2, dv)) { printf("%s\n", ast_last_error()); return 1; }
+    FILE* fp = fopen("delta_V", "w");
+    if (!fp) { printf("Cannot write delta_V\n"); return 1; }
+    for (int k = 0; k < NF; k++) fprintf(fp, "%8.4f\n", dv[k]);
+    fclose(fp);
+    /* The initial model state without the torque, BC and BW_BALL parameters (asteroid.c:913-941). */
+    fp = fopen("model_params.dat", "w");
+    if (!fp) { printf("Cannot write model_params.dat\n"); return 1; }
+    const ast_type_ids* T = &m->ids;
+    for (int j = 0; j < N; j++) {
+        const int ty = m->property[j][AST_P_TYPE];
+        if ((m->flags & AST_TORQUE) && (ty == T->Ti || ty == T->Ts || ty == T->Tl)) continue;
+        if ((m->flags & AST_BC) && (ty == T->c || ty == T->b)) continue;
+        if ((m->flags & AST_BW_BALL) && (ty == T->theta_R || ty == T->phi_R || ty == T->kappa)) continue;
+        fprintf(fp, "%15.11f ", params[j]);
+    }
+    fprintf(fp, "\n");
+    fclose(fp);
+    double* t = (double*)malloc(sizeof(double) * n_plot);
+    double* e = (double*)malloc(sizeof(double) * 3 * n_plot);
+    double* sv = (double*)malloc(sizeof(double) * 3 * n_plot);
+    double* vm = (double*)malloc(sizeof(double) * n_plot);
+    int rc = (!t || !e || !sv || !vm) ? 1 : 0;
+    if (!rc && (ast_plot_grid(hd, interp, n_plot, t, e, sv) || ast_model_curve_at(ctx, params, n_plot, t, e, sv, vm))) {
+        printf("%s\n", ast_last_error());
+        rc = 1;
+    }
+    if (!rc) {
+        /* "lsq" bins per-point values the default build never computes (asteroid.c:987-1025, on a
+         * freshly allocated, zero-filled array): 0 when all six time bins hold data, else nan. */
+        double cnt[6] = {0}, sum = 0, sw = 0;
+        for (int i = 0; i < hd->obs.n_data; i++) {
+            const double tt = hd->mjd[i];
+            cnt[tt < 0.5 ? 0 : tt < 1.5 ? 1 : tt < 2.7 ? 2 : tt < 3.7 ? 3 : tt < 4.5 ? 4 : 5] += 1;
+        }
+        for (int k = 0; k < 6; k++) {
+            const double W = (k == 2 || k == 3) ? 2 : 1;
+            sum = sum + W * (0.0 / cnt[k]);
+            sw = sw + W;
+        }
+        printf("chi2_plot = %13.6e, lsq = %13.6e\n", chi2, sqrt(sum / sw));
+        fp = fopen("model.dat", "w");
+        if (!fp) rc = 1;
+        else {
+            for (int i = 0; i < n_plot; i++) fprintf(fp, "%13.7f %13.6e\n", hd->hmjd0 + t[i], vm[i] + dv[0]);
+            fclose(fp);
+        }
+        fp = rc ? NULL : fopen("data.dat", "w");
+        if (!fp) rc = 1;
+        else {
+            /* V converted to the first filter (asteroid.c:1039-1045). */
+            for (int i = 0; i < hd->obs.n_data; i++)
+                fprintf(fp, "%13.7f %13.6e %13.6e w\n", hd->hmjd0 + hd->mjd[i], hd->v[i] - dv[hd->filter[i]] + dv[0],
+                        1 / sqrt(hd->w[i]));
+            fclose(fp);
+        }
+    }
+    free(t); free(e); free(sv); free(vm);
+    return rc;
 }
 
 int main(int argc, char** argv)
@@ -106,6 +182,7 @@ int main(int argc, char** argv)
     long long evals_cap = 0;
     const char *in = NULL, *outp = NULL, *eph = ".";
     int travel = 0, keep = 0, best = 0, reopt = 0, model_given = 0, plot = 0, Ncases = -1, Nstages = 1;
+    int n_plot = 20000; /* NPLOT (asteroid.h:266) */
     unsigned long seed = 0;
     int n_frozen = 0, n_limits = 0;
     int Fi[64], Li[64];
@@ -128,6 +205,7 @@ int main(int argc, char** argv)
             model_given = 1;
         }
         else if (!strcmp(a, "-plot")) { plot = 1; j++; }
+        else if (!strcmp(a, "-Nplot")) { NEED(1); n_plot = atoi(argv[j + 1]); j += 2; }
         else if (!strcmp(a, "-t")) { travel = 1; j++; }
         else if (!strcmp(a, "-reopt")) { reopt = 1; j++; }
         else if (!strcmp(a, "-keep")) { keep = 1; j++; }
@@ -150,7 +228,7 @@ int main(int argc, char** argv)
     if (!in) { printf("-i parameter is missing!\n"); return 1; }
     if ((reopt || plot) && !model_given) { printf("-reopt and -plot switches require -m switch!\n"); return 1; }
     if (!reopt && !plot && model_given) { printf("-m can only be used together with -reopt or -plot switches!\n"); return 1; }
-    if (plot) { printf("-plot is not part of this build's fitting path\n"); return 1; }
+    if (plot && n_plot < 2) { printf("Bad arguments!\n"); return 1; }
 
     ast_model model;
     if (ast_model_init(&model, flags, time_step, ppsi1, ppsi2)) { fprintf(stderr, "%s\n", ast_last_error()); return 1; }
@@ -178,6 +256,12 @@ int main(int argc, char** argv)
     }
     ast_ctx* ctx = NULL;
     if (ast_prepare(&model, &hd->obs, -1, &ctx)) { printf("%s\n", ast_last_error()); return 1; }
+    if (plot) {
+        const int rc = run_plot(&model, hd, ctx, params, (flags & AST_INTERP) != 0, n_plot);
+        ast_destroy(ctx);
+        ast_free_host_data(hd);
+        return rc;
+    }
     if (!outp) { printf("Bad output file name!\n"); return 1; }
     const int NF = hd->obs.n_filters;
     const long long n_chains = (long long)n_blocks * bsize;

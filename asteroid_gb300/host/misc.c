@@ -28,6 +28,34 @@ void ast_quadratic_interpolation(const double mjd0[3], const double e[3][3], con
     }
 }
 
+int ast_plot_grid(const ast_host_data* d, int32_t interp, int32_t n_plot, double* t, double* e_unit, double* s_unit)
+{
+    if (!d || !t || !e_unit || !s_unit || n_plot < 2)
+        return ast_set_error(AST_E_INVALID, "ast_plot_grid: bad argument");
+    const int64_t n = d->obs.n_data;
+    /* The ephemeris times of the grid are relative to hMJD0 in both modes (read_data.c:317-320). */
+    double mjd0[3];
+    for (int k = 0; k < 3; k++) mjd0[k] = interp ? d->obs.eph_mjd0[k] : d->obs.eph_mjd0[k] - d->hmjd0;
+    const double h = d->mjd[n - 1] / (n_plot - 1);
+    for (int32_t i = 0; i < n_plot; i++) {
+        double* ev = &e_unit[3 * i];
+        double* sv = &s_unit[3 * i];
+        if (i == 0 || i == n_plot - 1) {
+            /* The two ends are the first and the last observation (read_data.c:326-341). */
+            const int64_t j = i == 0 ? 0 : n - 1;
+            t[i] = d->mjd[j];
+            for (int k = 0; k < 3; k++) { ev[k] = d->e_unit[3 * j + k]; sv[k] = d->s_unit[3 * j + k]; }
+            continue;
+        }
+        t[i] = i * h;
+        ast_quadratic_interpolation(mjd0, d->obs.eph_e, d->obs.eph_s, t[i], ev, sv);
+        const double E = sqrt(ev[0] * ev[0] + ev[1] * ev[1] + ev[2] * ev[2]);
+        const double S = sqrt(sv[0] * sv[0] + sv[1] * sv[1] + sv[2] * sv[2]);
+        for (int k = 0; k < 3; k++) { ev[k] = ev[k] / E; sv[k] = sv[k] / S; }
+    }
+    return AST_OK;
+}
+
 int ast_read_minima(const char* path, ast_host_data* d)
 {
     if (!path || !d) return ast_set_error(AST_E_INVALID, "ast_read_minima: NULL argument");

@@ -175,6 +175,13 @@ void ast_free_host_data(ast_host_data* d);
 void ast_quadratic_interpolation(const double mjd0[3], const double e[3][3], const double s[3][3],
                                  double t, double out_e[3], double out_s[3]);
 
+/* read_data.c:309-370: the plot grid of -plot mode: n_plot times evenly spaced from the first to
+ * the last observation (relative to hMJD0), the two ends being those observations with their
+ * E and S, the interior E and S interpolated from the three ephemeris points and normalised.
+ * interp: the light curve was read with AST_INTERP. */
+int ast_plot_grid(const ast_host_data* d, int32_t interp, int32_t n_plot, double* t, double* e_unit,
+                  double* s_unit);
+
 /* asteroid.c:798-811: one result line "chi2 dV_1..dV_Nf p_1..p_N\n" with the reference's
  * "%13.6e " / "%15.11f " formats.  Returns the number of characters written. */
 int ast_format_result(char* buf, int64_t cap, double chi2, const double* dv, int32_t n_filters,
@@ -211,6 +218,13 @@ int ast_eval_batch_device(ast_ctx* ctx, int32_t precision, const double* d_param
  * (the reference's chi2one with Nplot > 0, cuda.c:699-704, without the delta_V shift):
  * the model-curve path of the plot mode and of the synthetic-data generator. */
 int ast_model_curve(ast_ctx* ctx, const double* params, double* vmod);
+
+/* The same model magnitudes at n other times t (relative to hMJD0, increasing, n >= 2) with
+ * unit E and S vectors e_unit, s_unit (ignored under AST_INTERP, where they are interpolated
+ * from the ephemeris as for the data): the model curve of -plot mode on its fine grid
+ * (chi2one with Nplot > 0 on dPlot, cuda.c:1949-1950), without the delta_V shift. */
+int ast_model_curve_at(ast_ctx* ctx, const double* params, int32_t n, const double* t, const double* e_unit,
+                       const double* s_unit, double* vmod);
 
 /* Euler angles (phi, theta, psi) at every observation, angles[3*i + k], as integrated by the
  * FP64 path or by the mixed path (double-float state, reduced to [-pi, pi] at each

@@ -73,3 +73,40 @@ def test_bad_arguments(gpu, data, tmp_path):
     assert rc == 1 and "-i parameter is missing" in out
     rc, out = run(["-i", str(data.dir / "lc.dat"), "-reopt", "-o", "x"], tmp_path)
     assert rc == 1 and "require -m" in out
+    rc, out = run(["-i", str(data.dir / "lc.dat"), "-plot"], tmp_path)
+    assert rc == 1 and "require -m" in out
+
+
+def test_plot_mode_files(gpu, data, tmp_path):
+    """-plot (asteroid.c:834-1060): delta_V, model_params.dat without the torque parameters,
+    model.dat on the Nplot grid shifted by delta_V[0], data.dat converted to the first filter."""
+    from asteroid_gb300 import api
+
+    d = data.dir
+    m = [f"{v:.12f}" for v in data.params_true]
+    rc, out = run(["-variant", "TORQUE,P_PSI,ACC", "-plot", "-Nplot", "500", "-i", str(d / "lc.dat"), "-eph", str(d),
+                   "-Ppsi", "2", "4800", "-m", *m], tmp_path)
+    assert rc == 0, out
+    assert "*** Plotting ***" in out
+    line = [l for l in out.splitlines() if l.startswith("chi2_plot = ")]
+    assert len(line) == 1
+    with api.Engine(data.model, data.obs) as eng:
+        chi2, dv = eng.eval(np.asarray(data.params_true)[None, :])
+        t, e, s = api.plot_grid(d / "lc.dat", d, 500)
+        vm = eng.model_curve_at(data.params_true, t, e, s)
+    assert float(line[0].split()[2].rstrip(",")) == float("%13.6e" % chi2[0])
+    assert float((tmp_path / "delta_V").read_text().split()[0]) == float("%8.4f" % dv[0, 0])
+    mp = (tmp_path / "model_params.dat").read_text().split()
+    ids = data.model.ids
+    keep = [j for j in range(data.model.n_params) if data.model.property[j][0] not in (ids.Ti, ids.Ts, ids.Tl)]
+    assert len(mp) == len(keep) == data.model.n_params - 3
+    assert np.allclose([float(x) for x in mp], np.asarray(data.params_true)[keep], rtol=0, atol=1e-10)
+    model = np.loadtxt(tmp_path / "model.dat")
+    assert model.shape == (500, 2)
+    assert np.allclose(model[:, 0], data.obs.hmjd0 + t, rtol=0, atol=1e-7)
+    assert np.allclose(model[:, 1], vm + dv[0, 0], rtol=1e-6, atol=0)
+    rows = [l.split() for l in (tmp_path / "data.dat").read_text().splitlines()]
+    assert len(rows) == data.obs.n_data and all(r[3] == "w" for r in rows)
+    dd = np.array([[float(x) for x in r[:3]] for r in rows])
+    assert np.allclose(dd[:, 1], data.obs.v - dv[0, data.obs.filt] + dv[0, 0], rtol=1e-6, atol=0)
+    assert np.allclose(dd[:, 2], 1 / np.sqrt(data.obs.w), rtol=1e-6, atol=0)

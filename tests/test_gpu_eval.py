@@ -12,7 +12,7 @@ own kernel (tests/test_ref_kernel.py), which shares the compiler and libm.
 import numpy as np
 import pytest
 
-from asteroid_gb300 import api
+from asteroid_gb300 import api, capi
 
 pytestmark = pytest.mark.gpu
 
@@ -119,3 +119,23 @@ def test_empty_batch(gpu, synth_objects):
     with api.Engine(s.model, s.obs) as eng:
         chi2, dv = eng.eval(np.zeros((0, s.model.n_params)))
     assert chi2.shape == (0,)
+
+
+@pytest.mark.parametrize("name", ["c0acc", "c1"])
+def test_model_curve_at_grid_matches_oracle(gpu, oracle_mod, synth_objects, name):
+    """-plot model curve (chi2one with Nplot > 0, cuda.c:1949-1950): at the data times it is the
+    data's model curve bit for bit; on the fine plot grid it is the oracle's curve there (under
+    INTERP both interpolate E and S from the ephemeris)."""
+    s = synth_objects(name)
+    interp = bool(s.model.flags & api.INTERP)
+    t, e, u = api.plot_grid(s.dir / "lc.dat", s.dir, 3 * s.obs.n_data, interp=interp)
+    with api.Engine(s.model, s.obs) as eng:
+        at_data = eng.model_curve_at(s.params_true, s.obs.mjd, s.obs.e_unit, s.obs.s_unit)
+        assert np.array_equal(at_data, eng.model_curve(s.params_true))
+        fine = eng.model_curve_at(s.params_true, t, e, u)
+        with pytest.raises(capi.AstError, match="increase"):
+            eng.model_curve_at(s.params_true, t[::-1], e, u)
+    grid = api.Obs(mjd=t, v=np.zeros(t.size), w=np.ones(t.size), filt=np.zeros(t.size), e_unit=e, s_unit=u,
+                   eph_e=s.obs.eph_e, eph_s=s.obs.eph_s, eph_mjd0=s.obs.eph_mjd0, hmjd0=s.obs.hmjd0)
+    ref = oracle_mod.model_curve(s.model, grid, s.params_true)
+    assert np.max(np.abs(fine - ref)) < 1e-9

@@ -155,3 +155,26 @@ def test_synthetic_generator_files(built, oracle_mod, tmp_path):
     assert s.obs.n_data == 300 and np.all(np.diff(s.obs.mjd) > 0)
     c, dv = oracle_mod.chi2(s.model, s.obs, s.params_true)
     assert 0.7 < c < 1.4
+
+
+@pytest.mark.parametrize("interp", [False, True])
+def test_plot_grid_follows_read_data(built, tmp_path, interp):
+    """-plot grid (read_data.c:309-370): ends = first/last observation, interior evenly spaced
+    with E, S interpolated in the last ephemeris window and normalised."""
+    eph_files(tmp_path, 58000.0, 58002.0)
+    rows = [("W", 58000.2, 20.0, 0.1), ("R", 58000.7, 21.0, 0.2), ("R", 58001.9, 21.5, 0.1)]
+    write_lc(tmp_path / "lc", rows)
+    o = api.read_data(tmp_path / "lc", tmp_path, interp=interp)
+    n_plot = 9
+    t, e, s = api.plot_grid(tmp_path / "lc", tmp_path, n_plot, interp=interp)
+    assert t[0] == o.mjd[0] == 0.0 and t[-1] == o.mjd[-1]
+    assert np.array_equal(e[0], o.e_unit[0]) and np.array_equal(s[-1], o.s_unit[-1])
+    h = o.mjd[-1] / (n_plot - 1)
+    assert np.array_equal(t[1:-1], np.arange(1, n_plot - 1) * h)
+    mjd0 = np.array([58000.0, 58001.0, 58002.0])
+    a = np.array([[1.0, 0.5, 0.0], [1.01, 0.51, 0.0], [1.02, 0.52, 0.0]])
+    E = synth._interp_vec(t[1:-1] + o.hmjd0, mjd0, np.array([[1.0, 0.0, 0.0], [1.0, 0.01, 0.0], [1.0, 0.02, 0.0]]) - a)
+    S = synth._interp_vec(t[1:-1] + o.hmjd0, mjd0, -a)
+    assert np.allclose(e[1:-1], E / np.linalg.norm(E, axis=1)[:, None], rtol=0, atol=1e-10)
+    assert np.allclose(s[1:-1], S / np.linalg.norm(S, axis=1)[:, None], rtol=0, atol=1e-10)
+    assert np.allclose(np.linalg.norm(e, axis=1), 1.0, atol=1e-14)
