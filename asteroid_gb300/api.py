@@ -183,6 +183,31 @@ def plot_grid(lc_path, eph_dir=".", n_plot: int = 20000, interp: bool = False):
         lib.ast_free_host_data(hd)
 
 
+@dataclass
+class PeriodogramResult:
+    cl_fr: np.ndarray       # [5] cluster frequencies (1/day), -1 where none
+    cl_H: np.ndarray        # [5] normalised counts there, 0 where none
+    counts: np.ndarray      # [10000] raw count of each frequency bin
+    n_minima: int
+    n_clusters: int
+    n_intervals: int
+    kernel_ms: float
+
+
+def minima(t, vm, device: int = -1) -> PeriodogramResult:
+    """Periodogram of the minima of a model curve (misc.c:65-276), on the GPU."""
+    lib = capi.load()
+    t = np.ascontiguousarray(t, dtype=np.float64)
+    vm = np.ascontiguousarray(vm, dtype=np.float64)
+    if t.shape != vm.shape:
+        raise ValueError("t and vm differ in length")
+    out = capi.Periodogram()
+    counts = np.zeros(capi.MINIMA_BINS, np.int32)
+    check(lib.ast_minima(int(device), int(t.size), dptr(t), dptr(vm), C.byref(out), iptr(counts)), "ast_minima")
+    return PeriodogramResult(np.array(out.cl_fr[:]), np.array(out.cl_H[:]), counts, out.n_minima, out.n_clusters,
+                             out.n_intervals, out.kernel_ms)
+
+
 def format_result(chi2, dv, params) -> str:
     """One output line in the reference's format (asteroid.c:798-811)."""
     lib = capi.load()

@@ -22,7 +22,7 @@ ORACLE_BUILD = ORACLE / "_build"
 
 ARCH = os.environ.get("AST_CUDA_ARCH", "sm_103a")
 GENCODE = [f"-gencode=arch=compute_{ARCH[3:]},code={ARCH}"]
-CU_SOURCES = ["csrc/engine.cu", "csrc/fit.cu", "csrc/batch.cu"]
+CU_SOURCES = ["csrc/engine.cu", "csrc/fit.cu", "csrc/batch.cu", "csrc/periodogram.cu"]
 C_SOURCES = ["host/tables.c", "host/read_data.c", "host/misc.c", "host/errors.c"]
 CLI_SOURCES = ["host/asteroid.c"]
 
@@ -74,7 +74,7 @@ def build_engine(force: bool = False, ptxas_verbose: bool = False) -> Path:
         o = BUILD / (s.stem + ".o")
         objs.append(o)
         if force or _stale(o, [s] + hdrs):
-            cmd = [nvcc, *GENCODE, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
+            cmd = [nvcc, *GENCODE, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
                    f"-I{INCLUDE}", f"-I{PKG / 'host'}", "-c", str(s), "-o", str(o)]
             if ptxas_verbose:
                 cmd.insert(1, "-Xptxas=-v")
@@ -84,7 +84,7 @@ def build_engine(force: bool = False, ptxas_verbose: bool = False) -> Path:
         o = BUILD / (s.stem + ".o")
         objs.append(o)
         if force or _stale(o, [s] + hdrs):
-            jobs.append(["gcc", "-O2", "-fPIC", "-std=c11", "-Wall", f"-I{INCLUDE}", f"-I{PKG / 'host'}",
+            jobs.append(["gcc", "-O2", "-fPIC", "-std=c11", "-Wall", "-ffp-contract=off", f"-I{INCLUDE}", f"-I{PKG / 'host'}",
                          "-c", str(s), "-o", str(o)])
     with ThreadPoolExecutor(max_workers=max(4, os.cpu_count() or 4)) as ex:
         list(ex.map(_run, jobs))
@@ -94,7 +94,7 @@ def build_engine(force: bool = False, ptxas_verbose: bool = False) -> Path:
     cli = BUILD / "asteroid"
     cli_src = [PKG / s for s in CLI_SOURCES if (PKG / s).exists()]
     if cli_src and (force or _stale(cli, cli_src + hdrs + [lib])):
-        _run(["gcc", "-O2", "-std=c11", "-Wall", f"-I{INCLUDE}", f"-I{PKG / 'host'}", *map(str, cli_src),
+        _run(["gcc", "-O2", "-std=c11", "-Wall", "-ffp-contract=off", f"-I{INCLUDE}", f"-I{PKG / 'host'}", *map(str, cli_src),
               "-o", str(cli), f"-L{BUILD}", "-lasteroid_gb300", f"-Wl,-rpath,{BUILD}", "-lm"])
     return lib
 
@@ -128,6 +128,8 @@ def build_reference_oracle() -> None:
         have = list((ORACLE / "_ref").glob("libref_*.so")) if (ORACLE / "_ref").exists() else []
         if not have:
             _run(["bash", str(script)])
+        elif not (ORACLE / "_ref" / "libref_minima.so").exists():
+            _run(["bash", str(script), "minima"])
 
 
 def build(force: bool = False) -> None:

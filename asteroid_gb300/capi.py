@@ -122,6 +122,20 @@ class BatchTune(C.Structure):
     ]
 
 
+class Periodogram(C.Structure):
+    _fields_ = [
+        ("n_minima", C.c_int32),
+        ("n_clusters", C.c_int32),
+        ("n_intervals", C.c_int64),
+        ("cl_fr", C.c_double * 5),
+        ("cl_H", C.c_double * 5),
+        ("kernel_ms", C.c_double),
+    ]
+
+
+MINIMA_BINS = 10000
+
+
 # Every function the header declares, with its ctypes signature.
 _P = C.c_void_p
 SIGNATURES = {
@@ -176,6 +190,8 @@ SIGNATURES = {
     "ast_batch_destroy": (None, [_P]),
     "ast_server_create": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int64, C.c_int64, C.POINTER(_P)]),
     "ast_server_set_lanes": (C.c_int, [_P, C.c_int32]),
+    "ast_minima": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                             C.POINTER(Periodogram), C.POINTER(C.c_int32)]),
     "ast_submit": (C.c_int, [_P, C.POINTER(Model), C.POINTER(ObsSet), C.POINTER(FitCfg), C.POINTER(C.c_int64)]),
     "ast_server_step": (C.c_int, [_P, C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "ast_poll": (C.c_int, [_P, C.c_int64, C.POINTER(FitOut), C.POINTER(C.c_double)]),

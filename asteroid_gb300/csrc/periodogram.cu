@@ -1,0 +1,247 @@
+// periodogram.cu -- the periodogram of model minima printed by -plot mode (minima(),
+// misc.c:65-276 of the reference, default build: no PARABOLIC_MAX, no MINIMA_SPLINE).
+//
+// The reference takes the brightness minima of the model curve on the plot grid, forms the
+// N(N-1)/2 intervals dt between every two of them, and for each of NN = 10000 trial frequencies
+// fr counts the intervals with |dt/(1/fr) - int(dt/(1/fr) + 0.5)| < 0.1 (misc.c:140-166).  That
+// count is the whole cost: NN x N(N-1)/2 tests, 1.2e9 for 500 minima and up to 5e11 at the
+// reference's cap of 10000 minima, run there on one host core.
+//
+// Here the count is one kernel on the FP32 pipe.  Each thread holds kFreqs frequencies as
+// double-float pairs; the intervals stream through shared memory, also as double-float pairs;
+// each test forms x = dt * fr as a double-float product (relative error ~2^-45), rounds its
+// high word to the nearest integer with the 1.5*2^23 addition, and takes the distance
+// |x_hi - r + x_lo| (x_hi - r is exact).  That distance is within kMarginBase + 1e-13 x of the
+// reference's, so every test farther than that from the 0.1 threshold is decided in float;
+// the few closer ones (a fraction of about 4e-7) are redone in FP64 exactly as the reference
+// writes them (dt / dt1 and int(x + 0.5) with dt1 = 1/fr), so every count is the reference's
+// bit for bit.  Counts are integers: the order in which threads add them is immaterial.  The
+// normalisation by mean and standard deviation and the cluster search stay on the host, in the
+// reference's order of operations (compiled without floating-point contraction).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+#include <algorithm>
+#include <vector>
+
+#include "asteroid_gb300.h"
+#include "engine.cuh"
+
+namespace ast {
+namespace {
+
+constexpr int kBins = AST_MINIMA_BINS;
+constexpr int kPeriodTpb = 256;
+constexpr int kFreqs = 4;                       // frequencies per thread
+constexpr int kFreqTile = kPeriodTpb * kFreqs;  // frequencies per CTA
+constexpr int kChunk = 2048;                    // intervals per shared-memory pass (16 KB)
+constexpr float kMarginBase = 1e-7f;            // rounding of x_hi - r + x_lo (<= 2^-25) and 0.1f vs 0.1
+// Periodogram constants of misc.c:131-135.
+constexpr double kSgm = 0.1, kDt0 = 1.0 / 24.0, kDt2 = 80.0 / 24.0, kS0 = 3;
+
+// Intervals between every two minima, in the reference's order (misc.c:106-121): pair (i, j),
+// i < j, at offset i*N - i(i+1)/2 + (j - i - 1).  One CTA per first minimum i.
+__global__ void pair_intervals_kernel(const double* __restrict__ tm, int n, double* __restrict__ dt)
+{
+    const int i = blockIdx.x;
+    if (i >= n - 1) return;
+    const int64_t base = (int64_t)i * n - (int64_t)i * (i + 1) / 2 - (i + 1);
+    const double ti = tm[i];
+    for (int j = i + 1 + threadIdx.x; j < n; j += blockDim.x) dt[base + j] = tm[j] - ti;
+}
+
+__device__ __forceinline__ float2 split_df(double v)
+{
+    const float hi = __double2float_rn(v);
+    return make_float2(hi, __double2float_rn(v - (double)hi));
+}
+
+// counts[f] += number of intervals in this CTA's slice within sgm of a whole number of periods.
+// grid: (frequency tiles, interval slices).
+__global__ void __launch_bounds__(kPeriodTpb) interval_count_kernel(const double* __restrict__ dt, int64_t m,
+                                                                     int64_t per_slice, const double* __restrict__ fr,
+                                                                     const double* __restrict__ dt1, int nn,
+                                                                     float margin, unsigned int* __restrict__ counts)
+{
+    __shared__ float2 s_dt[kChunk];
+    const int f0 = blockIdx.x * kFreqTile + threadIdx.x * kFreqs;
+    float fh[kFreqs], fl[kFreqs];
+    unsigned int cnt[kFreqs];
+#pragma unroll
+    for (int k = 0; k < kFreqs; k++) {
+        const float2 f = f0 + k < nn ? split_df(fr[f0 + k]) : make_float2(0.f, 0.f);
+        fh[k] = f.x;
+        fl[k] = f.y;
+        cnt[k] = 0;
+    }
+    const int64_t p0 = (int64_t)blockIdx.y * per_slice;
+    const int64_t p1 = min(m, p0 + per_slice);
+    const float lo_cut = 0.1f;
+    for (int64_t base = p0; base < p1; base += kChunk) {
+        const int n = (int)min((int64_t)kChunk, p1 - base);
+        __syncthreads();
+        for (int j = threadIdx.x; j < n; j += kPeriodTpb) s_dt[j] = split_df(dt[base + j]);
+        __syncthreads();
+        for (int j = 0; j < n; j++) {
+            const float2 d = s_dt[j];
+#pragma unroll
+            for (int k = 0; k < kFreqs; k++) {
+                const float xh = __fmul_rn(d.x, fh[k]);
+                float xl = __fmaf_rn(d.x, fh[k], -xh);
+                xl = __fmaf_rn(d.x, fl[k], xl);
+                xl = __fmaf_rn(d.y, fh[k], xl);
+                const float r = __fadd_rn(__fadd_rn(xh, 12582912.0f), -12582912.0f);
+                const float dd = fabsf(__fadd_rn(__fadd_rn(xh, -r), xl));
+                if (fabsf(__fadd_rn(dd, -lo_cut)) > margin || f0 + k >= nn) {
+                    cnt[k] += dd < lo_cut ? 1u : 0u;
+                } else {
+                    // Too close to call in float: the reference's own FP64 test (misc.c:145).
+                    const double x = dt[base + j] / dt1[f0 + k];
+                    const double dv = fabs(x - (double)(int)(x + 0.5));
+                    cnt[k] += dv < kSgm ? 1u : 0u;
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < kFreqs; k++)
+        if (f0 + k < nn && cnt[k]) atomicAdd(&counts[f0 + k], cnt[k]);
+}
+
+// Device buffers of one call, freed on every return.
+struct PeriodScratch {
+    double* tm = nullptr;
+    double* dt = nullptr;
+    double* fr = nullptr;
+    double* dt1 = nullptr;
+    unsigned int* counts = nullptr;
+    cudaStream_t s = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    ~PeriodScratch()
+    {
+        cudaFree(tm); cudaFree(dt); cudaFree(fr); cudaFree(dt1); cudaFree(counts);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        if (s) cudaStreamDestroy(s);
+    }
+};
+
+}  // namespace
+}  // namespace ast
+
+using namespace ast;
+
+extern "C" int ast_minima(int32_t device, int32_t n_plot, const double* t, const double* vm, ast_periodogram* out,
+                          int32_t* counts_out)
+{
+    if (!t || !vm || !out || n_plot < 0) return ast_set_error(AST_E_INVALID, "ast_minima: bad argument");
+    for (int32_t i = 1; i < n_plot; i++)
+        if (!(t[i] > t[i - 1])) return ast_set_error(AST_E_INVALID, "ast_minima: times must increase");
+    memset(out, 0, sizeof(*out));
+    // Minima of the curve at their grid times (misc.c:73-96).
+    std::vector<double> tm;
+    for (int32_t i = 1; i <= n_plot - 2; i++)
+        if (vm[i] > vm[i - 1] && vm[i] >= vm[i + 1]) {
+            if ((int)tm.size() >= AST_MINIMA_MAX)
+                return ast_set_error(AST_E_TOO_LARGE, "ast_minima: N>NMIN_MAX! (more than %d minima)", AST_MINIMA_MAX);
+            tm.push_back(t[i]);
+        }
+    const int n = (int)tm.size();
+    const int64_t m = (int64_t)n * (n - 1) / 2;
+    out->n_minima = n;
+    out->n_intervals = m;
+    // Trial frequencies (misc.c:137-144).
+    const double fr0 = 1 / kDt0, fr2 = 1 / kDt2;
+    std::vector<double> fr(kBins), dt1(kBins);
+    for (int i = 0; i < kBins; i++) {
+        fr[i] = fr2 + (double)i / (double)(kBins - 1) * (fr0 - fr2);
+        dt1[i] = 1 / fr[i];
+    }
+    std::vector<unsigned int> cnt(kBins, 0);
+    if (m > 0) {
+        // x = dt * fr must stay below 2^21 for the rounding of the count kernel.
+        const double x_max = (tm[n - 1] - tm[0]) * fr[kBins - 1];
+        if (!(x_max < 2097152.0))
+            return ast_set_error(AST_E_TOO_LARGE, "ast_minima: minima span %.6g days is too long", tm[n - 1] - tm[0]);
+        int rc = set_device(device);
+        if (rc) return rc;
+        PeriodScratch d;
+        if (cudaMalloc(&d.tm, sizeof(double) * n) != cudaSuccess || cudaMalloc(&d.dt, sizeof(double) * m) != cudaSuccess ||
+            cudaMalloc(&d.fr, sizeof(double) * kBins) != cudaSuccess ||
+            cudaMalloc(&d.dt1, sizeof(double) * kBins) != cudaSuccess ||
+            cudaMalloc(&d.counts, sizeof(unsigned int) * kBins) != cudaSuccess) {
+            cudaGetLastError();
+            return ast_set_error(AST_E_NOMEM, "ast_minima: cudaMalloc failed (%lld intervals)", (long long)m);
+        }
+        AST_CUDA(cudaStreamCreateWithFlags(&d.s, cudaStreamNonBlocking));
+        AST_CUDA(cudaEventCreate(&d.e0));
+        AST_CUDA(cudaEventCreate(&d.e1));
+        AST_CUDA(cudaMemcpyAsync(d.tm, tm.data(), sizeof(double) * n, cudaMemcpyHostToDevice, d.s));
+        AST_CUDA(cudaMemcpyAsync(d.fr, fr.data(), sizeof(double) * kBins, cudaMemcpyHostToDevice, d.s));
+        AST_CUDA(cudaMemcpyAsync(d.dt1, dt1.data(), sizeof(double) * kBins, cudaMemcpyHostToDevice, d.s));
+        AST_CUDA(cudaMemsetAsync(d.counts, 0, sizeof(unsigned int) * kBins, d.s));
+        pair_intervals_kernel<<<n - 1, 256, 0, d.s>>>(d.tm, n, d.dt);
+        AST_CUDA(cudaGetLastError());
+        int cur = 0, sms = 0;
+        AST_CUDA(cudaGetDevice(&cur));
+        AST_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cur));
+        const int tiles = (kBins + kFreqTile - 1) / kFreqTile;
+        // About eight CTAs per SM over all tiles, each slice at least 512 intervals.
+        int64_t slices = ((int64_t)sms * 8 + tiles - 1) / tiles;
+        slices = std::max<int64_t>(1, std::min<int64_t>(slices, (m + 511) / 512));
+        const int64_t per_slice = (m + slices - 1) / slices;
+        slices = (m + per_slice - 1) / per_slice;
+        const float margin = kMarginBase + (float)(1e-13 * x_max);
+        AST_CUDA(cudaEventRecord(d.e0, d.s));
+        interval_count_kernel<<<dim3(tiles, (unsigned)slices), kPeriodTpb, 0, d.s>>>(d.dt, m, per_slice, d.fr, d.dt1,
+                                                                                     kBins, margin, d.counts);
+        AST_CUDA(cudaGetLastError());
+        AST_CUDA(cudaEventRecord(d.e1, d.s));
+        AST_CUDA(cudaMemcpyAsync(cnt.data(), d.counts, sizeof(unsigned int) * kBins, cudaMemcpyDeviceToHost, d.s));
+        AST_CUDA(cudaStreamSynchronize(d.s));
+        float ms = 0;
+        AST_CUDA(cudaEventElapsedTime(&ms, d.e0, d.e1));
+        out->kernel_ms = ms;
+    }
+    // Normalisation and clusters (misc.c:170-268), in the reference's order.
+    std::vector<double> H(kBins);
+    std::vector<int> marked(kBins, 0);
+    double mean = 0.0;
+    for (int i = 0; i < kBins; i++) {
+        H[i] = (double)cnt[i];
+        mean = mean + H[i];
+        if (counts_out) counts_out[i] = (int32_t)cnt[i];
+    }
+    mean = mean / kBins;
+    double s = 0;
+    for (int i = 0; i < kBins; i++) {
+        const double dev = H[i] - mean;
+        s = s + dev * dev;
+    }
+    s = sqrt(s / (kBins - 1));
+    for (int i = 0; i < kBins; i++) H[i] = (H[i] - mean) / s;
+    int ncl = 0;
+    for (int j = 0; j < AST_NCL_MAX; j++) {
+        double top = -100;
+        int imax = -1;
+        out->cl_fr[j] = -1.0;
+        for (int i = 0; i < kBins; i++)
+            if (marked[i] == 0 && H[i] > top) {
+                top = H[i];
+                imax = i;
+            }
+        if (imax > -1 && H[imax] >= kS0) {
+            out->cl_fr[ncl] = fr[imax];
+            out->cl_H[ncl] = H[imax];
+            ncl++;
+            // The cluster extends both ways while the normalised count stays above s0.  (The
+            // reference's leftward walk from imax = 0 reads one element before the array; here
+            // it stops at the first bin.)
+            for (int i = imax; i < kBins && H[i] > kS0; i++) marked[i] = 1;
+            for (int i = imax - 1; i >= 0 && H[i] > kS0; i--) marked[i] = 1;
+        }
+    }
+    out->n_clusters = ncl;
+    return AST_OK;
+}

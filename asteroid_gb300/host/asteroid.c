@@ -103,8 +103,8 @@ static void usage(void)
 
 /* -plot mode (asteroid.c:834-1060, the default build): the chi^2 and delta_V of the -m model on
  * the data, the model curve on an evenly spaced grid of n_plot times shifted by delta_V of the
- * first filter, and the files delta_V, model_params.dat, model.dat and data.dat in the
- * reference's formats.  The model curve is the brightness model alone: NUDGE bookkeeping,
+ * first filter, the periodogram of that curve's minima (cluster frequencies and heights), and
+ * the files delta_V, model_params.dat, model.dat and data.dat in the reference's formats.  The model curve is the brightness model alone: NUDGE bookkeeping,
  * which in the reference can end the curve early after M_MAX minima, plays no part. */
 static int run_plot(const ast_model* m, const ast_host_data* hd, ast_ctx* ctx, const double* params, int interp,
                     int n_plot)
@@ -140,6 +140,20 @@ static int run_plot(const ast_model* m, const ast_host_data* hd, ast_ctx* ctx, c
         rc = 1;
     }
     if (!rc) {
+        /* The curve as the reference keeps it, shifted to the first filter (cuda.c:764). */
+        for (int i = 0; i < n_plot; i++) vm[i] = vm[i] + dv[0];
+        /* Periodogram of the model minima (asteroid.c:972-980). */
+        ast_periodogram pg;
+        if (ast_minima(-1, n_plot, t, vm, &pg, NULL)) {
+            printf("%s\n", ast_last_error());
+            rc = 1;
+        } else {
+            for (int j = 0; j < AST_NCL_MAX; j++) printf("%f ", pg.cl_fr[j]);
+            for (int j = 0; j < AST_NCL_MAX; j++) printf("%f ", pg.cl_H[j]);
+            printf("\n");
+        }
+    }
+    if (!rc) {
         /* "lsq" bins per-point values the default build never computes (asteroid.c:987-1025, on a
          * freshly allocated, zero-filled array): 0 when all six time bins hold data, else nan. */
         double cnt[6] = {0}, sum = 0, sw = 0;
@@ -156,7 +170,7 @@ static int run_plot(const ast_model* m, const ast_host_data* hd, ast_ctx* ctx, c
         fp = fopen("model.dat", "w");
         if (!fp) rc = 1;
         else {
-            for (int i = 0; i < n_plot; i++) fprintf(fp, "%13.7f %13.6e\n", hd->hmjd0 + t[i], vm[i] + dv[0]);
+            for (int i = 0; i < n_plot; i++) fprintf(fp, "%13.7f %13.6e\n", hd->hmjd0 + t[i], vm[i]);
             fclose(fp);
         }
         fp = rc ? NULL : fopen("data.dat", "w");

@@ -231,6 +231,32 @@ int ast_model_curve_at(ast_ctx* ctx, const double* params, int32_t n, const doub
  * observation): the phase drift of the mixed path.  No reference counterpart. */
 int ast_model_angles(ast_ctx* ctx, int32_t precision, const double* params, double* angles);
 
+/* The periodogram of model minima printed by -plot mode: minima() (misc.c:65-276, default
+ * build).  The brightness minima of a model curve (V[i] > V[i-1] && V[i] >= V[i+1]) are taken at
+ * their grid times; every interval between two of them is tested against AST_MINIMA_BINS trial
+ * frequencies fr evenly spaced from 24/80 to 24 per day: it counts for fr when it lies within
+ * 0.1 of a whole number of periods 1/fr.  The counts, normalised by their mean and standard
+ * deviation, give the AST_NCL_MAX highest clusters at or above 3 (cl_fr, cl_H; -1 and 0 where
+ * there are fewer), which asteroid.c:974-980 prints.  At most AST_MINIMA_MAX minima
+ * (NMIN_MAX; more is AST_E_TOO_LARGE, where the reference exits). */
+#define AST_MINIMA_BINS 10000 /* NN, misc.c:131 */
+#define AST_NCL_MAX     5     /* NCL_MAX, asteroid.h:277 */
+#define AST_MINIMA_MAX  10000 /* NMIN_MAX, misc.c:69 */
+
+typedef struct ast_periodogram {
+    int32_t n_minima;          /* minima found on the curve */
+    int32_t n_clusters;        /* clusters found (<= AST_NCL_MAX) */
+    int64_t n_intervals;       /* n_minima (n_minima - 1) / 2 */
+    double  cl_fr[AST_NCL_MAX];  /* cluster frequency (1/day), -1 where none */
+    double  cl_H[AST_NCL_MAX];   /* normalised count at that frequency, 0 where none */
+    double  kernel_ms;         /* device time of the interval test */
+} ast_periodogram;
+
+/* Curve vm at n_plot increasing times t (days) on CUDA device `device` (-1: current).  counts
+ * (optional, AST_MINIMA_BINS entries) receives the raw count of each frequency bin. */
+int ast_minima(int32_t device, int32_t n_plot, const double* t, const double* vm, ast_periodogram* out,
+               int32_t* counts);
+
 typedef struct ast_fit_cfg {
     uint64_t seed;          /* -seed; chains draw from Philox4x32-10 keyed by (seed, chain) */
     int64_t  n_chains;      /* N_BLOCKS*BSIZE in the reference */

@@ -8,6 +8,8 @@
 #   ref_<variant>.cubin  device build (sm_100) of the same functions plus
 #                        oracle/ref_harness_kernel.cu; loaded on the GPU by
 #                        oracle/ref_gpu_loader.cpp to check the CUDA path at 1e-12.
+#   libref_minima.so     host build of minima() (misc.c:65-276, default macros) with
+#                        oracle/ref_harness_minima.cu; pins the periodogram oracle.
 #
 # The reference's asteroid.h and cuda.c are streamed through sed into nvcc's standard input:
 # the four device functions become __host__ __device__ (host build only), N_FILTERS becomes 8
@@ -55,6 +57,15 @@ stream_source() {  # $1 = time step, $2 = 1 for the host build
 }
 
 pids=()
+if [[ -f "$REF/misc.c" && ( "${1:-all}" == "all" || "${1:-all}" == "host" || "${1:-all}" == "minima" ) ]]; then
+    ( { sed -e 's/^const int N_FILTERS = 1;/const int N_FILTERS = 8;/' "$REF/asteroid.h"
+        sed -e 's/^#include "asteroid.h"//' "$REF/misc.c"
+        cat "$here/ref_harness_minima.cu"; } |
+      nvcc -x cu -arch=sm_100 -O2 -DMAIN -I"$REF" -Xcompiler -fPIC,-ffp-contract=off -shared -w \
+           -o "$OUT/libref_minima.so" - ) &
+    pids+=($!)
+fi
+[[ "${1:-all}" == "minima" ]] && VARIANTS=()
 for v in "${VARIANTS[@]}"; do
     read -r name ts macros <<<"$v"
     if [[ "${1:-all}" == "all" || "${1:-all}" == "host" ]]; then

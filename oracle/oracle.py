@@ -47,6 +47,8 @@ def load():
         lib.orc_philox4x32_10.restype = None
         lib.orc_philox4x32_10.argtypes = [V, V, V]
         lib.orc_max_threads.restype = C.c_int
+        lib.orc_minima.restype = C.c_int
+        lib.orc_minima.argtypes = [V, V, C.c_int, C.c_int, V, V, V, V]
         lib.orc_fit.restype = None
         lib.orc_fit.argtypes = [V, V, C.c_uint64, C.c_int64, C.c_int32, C.c_int32, C.c_int32, V, C.c_int64, C.c_int32,
                                 V, V, V, V, V]
@@ -87,6 +89,22 @@ def model_curve(model, obs, params):
     out = np.zeros(obs.n_data)
     lib.orc_model_curve(mp, op, p.ctypes.data, out.ctypes.data)
     return out
+
+
+def minima(t, vm, threads: int = 0):
+    """Periodogram of model minima (misc.c:65-276): (cl_fr[5], cl_H[5], counts[10000], n_minima)."""
+    lib = load()
+    t = np.ascontiguousarray(t, dtype=np.float64)
+    vm = np.ascontiguousarray(vm, dtype=np.float64)
+    fr = np.zeros(5)
+    h = np.zeros(5)
+    counts = np.zeros(10000, np.int32)
+    n = np.zeros(1, np.int32)
+    rc = lib.orc_minima(t.ctypes.data, vm.ctypes.data, int(t.size), int(threads or max_threads()), fr.ctypes.data,
+                        h.ctypes.data, counts.ctypes.data, n.ctypes.data)
+    if rc < 0:
+        raise ValueError("more than 10000 minima")
+    return fr, h, counts, int(n[0])
 
 
 def x2params(model, x, reopt=1):
