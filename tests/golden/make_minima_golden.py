@@ -1,4 +1,4 @@
-"""Generate tests/golden/ref_minima.json from the reference's own minima() (misc.c:65-276).
+"""Generate tests/golden/minima_ref.json from the reference's own minima() (misc.c:65-276).
 
 Run here, where the reference checkout exists:  bash oracle/build_ref.sh minima && python
 tests/golden/make_minima_golden.py.  Each case is a curve on a plot-style grid t[i] = i * h,
@@ -59,7 +59,7 @@ def main():
         print(kind, nmin, fr, H)
     doc = {"generator": "tests/golden/make_minima_golden.py from the reference host build oracle/_ref/libref_minima.so",
            "cases": out}
-    (Path(__file__).resolve().parent / "ref_minima.json").write_text(json.dumps(doc))
+    (Path(__file__).resolve().parent / "minima_ref.json").write_text(json.dumps(doc))
 
 
 if __name__ == "__main__":

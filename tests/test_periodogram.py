@@ -11,7 +11,7 @@ import pytest
 from asteroid_gb300 import api, capi
 
 ROOT = Path(__file__).resolve().parents[1]
-GOLDEN = json.loads((ROOT / "tests" / "golden" / "ref_minima.json").read_text())["cases"]
+GOLDEN = json.loads((ROOT / "tests" / "golden" / "minima_ref.json").read_text())["cases"]
 REF_LIB = ROOT / "oracle" / "_ref" / "libref_minima.so"
 
 
