@@ -352,6 +352,95 @@ def bench_batch(args, tmp, rank, world):
     print(json.dumps(line))
 
 
+def periodogram_curve():
+    """The periodogram workload: a 20000-point plot grid (NPLOT) over 60 days carrying a 0.21-day
+    double wave with noise, 4809 minima, 1.16e7 intervals: 1.16e11 interval tests per call."""
+    n, span = 20000, 60.0
+    rng = np.random.default_rng(22)
+    t = np.arange(n) * (span / (n - 1))
+    return t, 0.3 * np.sin(2 * np.pi * t / 0.21) + 0.02 * rng.standard_normal(n)
+
+
+# FP32-pipe lane instructions of one interval test in the count kernel: the double-float product
+# (FMUL + 3 FFMA), the rounding to the nearest integer (2 FADD), the distance (2 FADD), the
+# threshold test (FADD + FSETP).
+PERIODOGRAM_FP32_OPS = 10
+
+
+def bench_periodogram(args, tmp, rank, world):
+    """The periodogram of model minima of -plot mode (minima(), misc.c:65-276): interval tests/s
+    of the CUDA count, the same through ast_minima with host buffers, and the -plot sequence of
+    the config-2 object (model curve on the 20000-point grid, then the periodogram)."""
+    import torch
+
+    from asteroid_gb300 import api, synth
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    t, vm = periodogram_curve()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")
+    for _ in range(max(args.warmup, 3)):
+        r = api.minima(t, vm, device=local)
+    kernel_ms, call_s = [], []
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r = api.minima(t, vm, device=local)
+            call_s.append(time.perf_counter() - t0)
+            kernel_ms.append(r.kernel_ms)
+    tests = r.n_intervals * 10000
+    value = tests / (statistics.mean(kernel_ms) * 1e-3)
+    e2e = tests / statistics.mean(call_s)
+    if args.profile:   # the periodogram calls only (for ncu)
+        print(json.dumps({"mode": "periodogram", "value": value, "unit": "tests/s", "kernel_ms": kernel_ms}))
+        return
+    peak_ops = api.probe_peak("fp32", local) * 1e9 / 2   # FMA lane instructions/s
+    achieved = value * PERIODOGRAM_FP32_OPS
+    line = {"metric": "interval_tests_per_s", "value": value, "unit": "tests/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": statistics.mean(kernel_ms), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (double-float) + f64 fallback",
+            "data": "synthetic", "mode": "periodogram",
+            "config": {"workload": "minima() periodogram of a 20000-point plot curve, 60 days, "
+                                   f"{r.n_minima} minima, {r.n_intervals} intervals x 10000 frequencies",
+                       "l2": "flushed (256 MB write) before each call; the count kernel is compute-bound"},
+            "clocks": clk.summary(), "gpu_launches": 2 * args.steps,
+            "e2e": {"value": e2e, "unit": "tests/s", "h2d_bytes_per_step": 16 * t.size,
+                    "d2h_bytes_per_step": 4 * 10000},
+            "roofline": {"bound": "fp32 pipe (CUDA cores)", "achieved": achieved / 1e12,
+                         "peak": peak_ops / 1e12, "unit": "T lane-ops/s", "frac": achieved / peak_ops,
+                         "traffic": None,
+                         "note": f"{PERIODOGRAM_FP32_OPS} FP32-pipe lane instructions per test; peak = the "
+                                 "FMA rate measured by ast_probe_peak in this run, in instructions"},
+            "result": {"cl_fr": list(r.cl_fr), "cl_H": list(r.cl_H)}}
+    # CPU: the oracle port on all host threads, on the same curve (about 15 s on 16 cores).
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+
+    threads = O.max_threads()
+    t0 = time.perf_counter()
+    fr, h, counts, n_min = O.minima(t, vm, threads=threads)
+    cpu_s = time.perf_counter() - t0
+    line["cpu_baseline"] = {"value": tests / cpu_s, "unit": "tests/s", "cores": threads, "kind": "port",
+                            "sample": "the whole workload once (the reference's own minima() is single-threaded)"}
+    line["parity"] = {"counts_equal_oracle": bool(np.array_equal(counts, r.counts)),
+                      "clusters_equal_oracle": bool(np.array_equal(fr, r.cl_fr) and np.array_equal(h, r.cl_H))}
+    # The -plot sequence on the config-2 object, through the public API.
+    s = synth.generate("c2", tmp)
+    with api.Engine(s.model, s.obs, device=local) as eng:
+        tg, eg, sg = api.plot_grid(s.dir / "lc.dat", s.dir, 20000, interp=True)
+        _, dv = eng.eval(np.asarray(s.params_true)[None, :])
+        eng.model_curve_at(s.params_true, tg, eg, sg)
+        t0 = time.perf_counter()
+        curve = eng.model_curve_at(s.params_true, tg, eg, sg) + dv[0, 0]
+        t1 = time.perf_counter()
+        rp = api.minima(tg, curve, device=local)
+        t2 = time.perf_counter()
+    line["plot_c2"] = {"model_curve_ms": 1e3 * (t1 - t0), "minima_ms": 1e3 * (t2 - t1), "n_minima": rp.n_minima,
+                       "cl_fr": list(rp.cl_fr)}
+    print(json.dumps(line))
+
+
 def bench_serve(args, tmp, rank, world):
     """Config 4: Poisson arrivals of config-3 objects (1024 chains x 5000 evaluations each) at 1, 4,
     16 and 64 requests/s into one server (150 GB HBM budget); p50/p99 latency from submission to
@@ -450,10 +539,10 @@ def main():
     ap.add_argument("--budget-fp64", type=int, default=0)
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-batched", action="store_true")
-    ap.add_argument("--mode", default="fit", choices=["fit", "batch", "serve", "compare"],
+    ap.add_argument("--mode", default="fit", choices=["fit", "batch", "serve", "compare", "periodogram"],
                     help="fit: the headline line; batch: config 3 (uneven objects, one launch); "
                          "serve: config 4 (Poisson arrivals, continuous batching); compare: full fits of "
-                         "--config in both precisions at one seed")
+                         "--config in both precisions at one seed; periodogram: minima() of plot mode")
     ap.add_argument("--objects", type=int, default=512, help="batch mode: objects")
     ap.add_argument("--requests", type=int, default=8, help="serve mode: requests per arrival rate")
     ap.add_argument("--lanes", type=int, default=1, choices=[1, 4], help="serve mode: lanes per chain")
@@ -515,6 +604,8 @@ def main():
         return bench_serve(args, tmp, rank, world)
     if args.mode == "compare":
         return bench_compare(args, tmp, rank, world)
+    if args.mode == "periodogram":
+        return bench_periodogram(args, tmp, rank, world)
     s = make_workload(args, tmp)
     model, obs = s.model, s.obs
     eng = api.Engine(model, obs, device=local)
