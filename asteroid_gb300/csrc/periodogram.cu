@@ -33,7 +33,7 @@ namespace {
 
 constexpr int kBins = AST_MINIMA_BINS;
 constexpr int kPeriodTpb = 256;
-constexpr int kFreqs = 4;                       // frequencies per thread
+constexpr int kFreqs = 8;                       // frequencies per thread
 constexpr int kFreqTile = kPeriodTpb * kFreqs;  // frequencies per CTA
 constexpr int kChunk = 2048;                    // intervals per shared-memory pass (16 KB)
 constexpr float kMarginBase = 1e-7f;            // rounding of x_hi - r + x_lo (<= 2^-25) and 0.1f vs 0.1
@@ -57,56 +57,110 @@ __device__ __forceinline__ float2 split_df(double v)
     return make_float2(hi, __double2float_rn(v - (double)hi));
 }
 
+constexpr float kRound = 12582912.0f;  // 1.5 * 2^23: x + kRound - kRound is x rounded to an integer
+
+// The decision for one interval and frequency when the fast test is too close to call:
+// the double-float distance (error < kMarginBase + 1e-13 x), and where even that is too close,
+// the reference's own FP64 test (misc.c:145).  Returns 1 if the interval counts.
+__device__ __noinline__ unsigned int precise_test(float dth, float dtl, float fh, float fl, double dt, double dt1,
+                                                  float margin)
+{
+    const float xh = __fmul_rn(dth, fh);
+    float xl = __fmaf_rn(dth, fh, -xh);
+    xl = __fmaf_rn(dth, fl, xl);
+    xl = __fmaf_rn(dtl, fh, xl);
+    const float r = __fadd_rn(__fadd_rn(xh, kRound), -kRound);
+    const float dd = fabsf(__fadd_rn(__fadd_rn(xh, -r), xl));
+    if (fabsf(__fadd_rn(dd, -0.1f)) > margin) return dd < 0.1f ? 1u : 0u;
+    const double x = dt / dt1;
+    const double dv = fabs(x - (double)(int)(x + 0.5));
+    return dv < kSgm ? 1u : 0u;
+}
+
 // counts[f] += number of intervals in this CTA's slice within sgm of a whole number of periods.
 // grid: (frequency tiles, interval slices).
+//
+// Fast test of interval dt_h against frequency f_h, four FP32 instructions: y = fma(dt_h, f_h,
+// 1.5*2^23) rounds the exact product p to the nearest integer r; d = fma(dt_h, f_h, -r) is p - r
+// with one rounding; a = |d| - 0.1.  The interval counts when a < 0 (its sign bit is added).  The
+// error of a against the reference's |x - int(x + 0.5)| - 0.1 is below 1.2e-7 x + 3.2e-8 (the
+// float rounding of dt and fr, then two roundings of at most 2^-26); each interval's bound
+// dt_h * (2.4e-7 max f_h) + 1e-7 covers twice that.  The smallest |a| of the thread's frequencies is
+// kept, and only when it is within the bound does the warp take the precise test, for the
+// frequencies that need it, correcting the count by the difference of the two decisions.
+__device__ __forceinline__ void test_interval(float dth, int j, const float* s_dtl, int64_t base,
+                                              const double* __restrict__ dt, const double* __restrict__ dt1, int f0,
+                                              int nn, const float (&fh)[kFreqs], const float (&fl)[kFreqs], float thr,
+                                              float margin, int (&cnt)[kFreqs])
+{
+    float a[kFreqs];
+    float amin = 1.0f;
+#pragma unroll
+    for (int k = 0; k < kFreqs; k++) {
+        const float y = __fmaf_rn(dth, fh[k], kRound);
+        const float r = __fadd_rn(y, -kRound);
+        const float d = __fmaf_rn(dth, fh[k], -r);
+        a[k] = __fadd_rn(fabsf(d), -0.1f);
+        cnt[k] += (int)(__float_as_uint(a[k]) >> 31);
+        amin = fminf(amin, fabsf(a[k]));
+    }
+    const float bound = __fmaf_rn(dth, thr, kMarginBase);
+    if (amin <= bound) {
+        const float dtl = s_dtl[j];
+        const double dtd = dt[base + j];
+#pragma unroll
+        for (int k = 0; k < kFreqs; k++)
+            if (fabsf(a[k]) <= bound && f0 + k < nn) {
+                const int fast = (int)(__float_as_uint(a[k]) >> 31);
+                cnt[k] += (int)precise_test(dth, dtl, fh[k], fl[k], dtd, dt1[f0 + k], margin) - fast;
+            }
+    }
+}
+
 __global__ void __launch_bounds__(kPeriodTpb) interval_count_kernel(const double* __restrict__ dt, int64_t m,
                                                                      int64_t per_slice, const double* __restrict__ fr,
                                                                      const double* __restrict__ dt1, int nn,
                                                                      float margin, unsigned int* __restrict__ counts)
 {
-    __shared__ float2 s_dt[kChunk];
+    __shared__ __align__(16) float s_dth[kChunk];
+    __shared__ float s_dtl[kChunk];
     const int f0 = blockIdx.x * kFreqTile + threadIdx.x * kFreqs;
     float fh[kFreqs], fl[kFreqs];
-    unsigned int cnt[kFreqs];
+    int cnt[kFreqs];
+    float fmax = 0.0f;
 #pragma unroll
     for (int k = 0; k < kFreqs; k++) {
         const float2 f = f0 + k < nn ? split_df(fr[f0 + k]) : make_float2(0.f, 0.f);
         fh[k] = f.x;
         fl[k] = f.y;
         cnt[k] = 0;
+        fmax = fmaxf(fmax, f.x);
     }
+    const float thr = fmax * 2.4e-7f;
     const int64_t p0 = (int64_t)blockIdx.y * per_slice;
     const int64_t p1 = min(m, p0 + per_slice);
-    const float lo_cut = 0.1f;
     for (int64_t base = p0; base < p1; base += kChunk) {
         const int n = (int)min((int64_t)kChunk, p1 - base);
         __syncthreads();
-        for (int j = threadIdx.x; j < n; j += kPeriodTpb) s_dt[j] = split_df(dt[base + j]);
-        __syncthreads();
-        for (int j = 0; j < n; j++) {
-            const float2 d = s_dt[j];
-#pragma unroll
-            for (int k = 0; k < kFreqs; k++) {
-                const float xh = __fmul_rn(d.x, fh[k]);
-                float xl = __fmaf_rn(d.x, fh[k], -xh);
-                xl = __fmaf_rn(d.x, fl[k], xl);
-                xl = __fmaf_rn(d.y, fh[k], xl);
-                const float r = __fadd_rn(__fadd_rn(xh, 12582912.0f), -12582912.0f);
-                const float dd = fabsf(__fadd_rn(__fadd_rn(xh, -r), xl));
-                if (fabsf(__fadd_rn(dd, -lo_cut)) > margin || f0 + k >= nn) {
-                    cnt[k] += dd < lo_cut ? 1u : 0u;
-                } else {
-                    // Too close to call in float: the reference's own FP64 test (misc.c:145).
-                    const double x = dt[base + j] / dt1[f0 + k];
-                    const double dv = fabs(x - (double)(int)(x + 0.5));
-                    cnt[k] += dv < kSgm ? 1u : 0u;
-                }
-            }
+        for (int j = threadIdx.x; j < n; j += kPeriodTpb) {
+            const float2 d = split_df(dt[base + j]);
+            s_dth[j] = d.x;
+            s_dtl[j] = d.y;
         }
+        __syncthreads();
+        const int n4 = n & ~3;
+        for (int j = 0; j < n4; j += 4) {
+            const float4 d4 = *reinterpret_cast<const float4*>(&s_dth[j]);
+            test_interval(d4.x, j, s_dtl, base, dt, dt1, f0, nn, fh, fl, thr, margin, cnt);
+            test_interval(d4.y, j + 1, s_dtl, base, dt, dt1, f0, nn, fh, fl, thr, margin, cnt);
+            test_interval(d4.z, j + 2, s_dtl, base, dt, dt1, f0, nn, fh, fl, thr, margin, cnt);
+            test_interval(d4.w, j + 3, s_dtl, base, dt, dt1, f0, nn, fh, fl, thr, margin, cnt);
+        }
+        for (int j = n4; j < n; j++) test_interval(s_dth[j], j, s_dtl, base, dt, dt1, f0, nn, fh, fl, thr, margin, cnt);
     }
 #pragma unroll
     for (int k = 0; k < kFreqs; k++)
-        if (f0 + k < nn && cnt[k]) atomicAdd(&counts[f0 + k], cnt[k]);
+        if (f0 + k < nn && cnt[k]) atomicAdd(&counts[f0 + k], (unsigned int)cnt[k]);
 }
 
 // Device buffers of one call, freed on every return.
