@@ -241,8 +241,11 @@ extern "C" int ast_minima(int32_t device, int32_t n_plot, const double* t, const
         AST_CUDA(cudaGetDevice(&cur));
         AST_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cur));
         const int tiles = (kBins + kFreqTile - 1) / kFreqTile;
-        // About eight CTAs per SM over all tiles, each slice at least 512 intervals.
-        int64_t slices = ((int64_t)sms * 8 + tiles - 1) / tiles;
+        // One wave: as many (tile, slice) CTAs as are resident at once, all with the same work
+        // (each slice at least 512 intervals).
+        int occ = 0;
+        AST_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, interval_count_kernel, kPeriodTpb, 0));
+        int64_t slices = std::max<int64_t>(1, (int64_t)sms * std::max(occ, 1) / tiles);
         slices = std::max<int64_t>(1, std::min<int64_t>(slices, (m + 511) / 512));
         const int64_t per_slice = (m + slices - 1) / slices;
         slices = (m + per_slice - 1) / per_slice;

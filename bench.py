@@ -361,10 +361,10 @@ def periodogram_curve():
     return t, 0.3 * np.sin(2 * np.pi * t / 0.21) + 0.02 * rng.standard_normal(n)
 
 
-# FP32-pipe lane instructions of one interval test in the count kernel: the double-float product
-# (FMUL + 3 FFMA), the rounding to the nearest integer (2 FADD), the distance (2 FADD), the
-# threshold test (FADD + FSETP).
-PERIODOGRAM_FP32_OPS = 10
+# Lane instructions of one interval test in the count kernel's fast path: the product rounded to
+# an integer (FFMA + FADD), the remainder (FFMA), its distance to the threshold (FADD), the sign
+# bit added to the count (IADD) and the smallest distance kept (FMNMX).
+PERIODOGRAM_OPS = 6
 
 
 def bench_periodogram(args, tmp, rank, world):
@@ -395,8 +395,8 @@ def bench_periodogram(args, tmp, rank, world):
     if args.profile:   # the periodogram calls only (for ncu)
         print(json.dumps({"mode": "periodogram", "value": value, "unit": "tests/s", "kernel_ms": kernel_ms}))
         return
-    peak_ops = api.probe_peak("fp32", local) * 1e9 / 2   # FMA lane instructions/s
-    achieved = value * PERIODOGRAM_FP32_OPS
+    peak_ops = api.probe_peak("fp32", local) * 1e9 / 2   # FMA lane instructions/s: the issue rate
+    achieved = value * PERIODOGRAM_OPS
     line = {"metric": "interval_tests_per_s", "value": value, "unit": "tests/s", "n_gpus": 1, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": statistics.mean(kernel_ms), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (double-float) + f64 fallback",
@@ -407,11 +407,12 @@ def bench_periodogram(args, tmp, rank, world):
             "clocks": clk.summary(), "gpu_launches": 2 * args.steps,
             "e2e": {"value": e2e, "unit": "tests/s", "h2d_bytes_per_step": 16 * t.size,
                     "d2h_bytes_per_step": 4 * 10000},
-            "roofline": {"bound": "fp32 pipe (CUDA cores)", "achieved": achieved / 1e12,
+            "roofline": {"bound": "instruction issue (FP32 + ALU pipes, CUDA cores)", "achieved": achieved / 1e12,
                          "peak": peak_ops / 1e12, "unit": "T lane-ops/s", "frac": achieved / peak_ops,
                          "traffic": None,
-                         "note": f"{PERIODOGRAM_FP32_OPS} FP32-pipe lane instructions per test; peak = the "
-                                 "FMA rate measured by ast_probe_peak in this run, in instructions"},
+                         "note": f"{PERIODOGRAM_OPS} lane instructions per test (the fast path); peak = one "
+                                 "warp instruction per SM sub-partition per clock, taken as the FP32 FMA rate "
+                                 "measured by ast_probe_peak in this run"},
             "result": {"cl_fr": list(r.cl_fr), "cl_H": list(r.cl_H)}}
     # CPU: the oracle port on all host threads, on the same curve (about 15 s on 16 cores).
     sys.path.insert(0, str(ROOT / "oracle"))
