@@ -18,9 +18,9 @@ AST_MAX_FILTERS = 8
 AST_NOBS_MAX = 10
 AST_N_COLUMNS = 6
 
-TORQUE, BC, BW_BALL, P_PSI, INTERP, ACC, NUDGE = 0x01, 0x02, 0x04, 0x08, 0x10, 0x20, 0x40
+TORQUE, BC, BW_BALL, P_PSI, INTERP, ACC, NUDGE, RMSD = 0x01, 0x02, 0x04, 0x08, 0x10, 0x20, 0x40, 0x80
 FLAG_NAMES = {"TORQUE": TORQUE, "BC": BC, "BW_BALL": BW_BALL, "P_PSI": P_PSI,
-              "INTERP": INTERP, "ACC": ACC, "NUDGE": NUDGE}
+              "INTERP": INTERP, "ACC": ACC, "NUDGE": NUDGE, "RMSD": RMSD}
 PREC_FP64, PREC_MIXED = 0, 1
 
 STATUS = {0: "AST_OK", -1: "AST_E_INVALID", -2: "AST_E_NOMEM", -3: "AST_E_CUDA", -4: "AST_E_IO",

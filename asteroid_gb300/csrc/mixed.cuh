@@ -539,15 +539,19 @@ __host__ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const dou
     }
     if ((flags & AST_NUDGE) && !nudge_flush(M, o, F, tab, cand, &n_cand, &Mmin, t_mod, V_mod)) return (CF)kHuge;
 #undef AST_P
-    CF chi2m, chi2a = 0.0;
+    CF chi2m, chi2a = 0.0, SUM_w = 0.0;
     CF dv[AST_MAX_FILTERS];
     for (int m = 0; m < N_filters; m++) {
         const double sy = df_to_double(sum_y[m]), sy2 = df_to_double(sum_y2[m]), sw = o.sum_w[m];
         chi2m = (CF)DD_SUB(sy2, DD_MUL(sy, sy) / sw);
         chi2a = chi2a + chi2m;
         dv[m] = (CF)(sy / sw);
+        SUM_w = (CF)DD_ADD((double)SUM_w, sw);
     }
-    chi2a = chi2a / (CF)(N_data - M.n_params - N_filters);
+    if (flags & AST_RMSD)
+        chi2a = sqrt(chi2a / SUM_w);
+    else
+        chi2a = chi2a / (CF)(N_data - M.n_params - N_filters);
     if (flags & AST_NUDGE) {
         float S_M = 0.0f, P_tot = 1.0f;
         for (int imod = 0; imod < Mmin; imod++) {

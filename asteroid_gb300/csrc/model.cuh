@@ -551,15 +551,20 @@ __device__ CF chi2_fp64(const DevModel& M, const ObsView& o, const double* param
     }
 #undef AST_P
 
-    // Per-filter chi^2 and delta_V (cuda.c:887-910).
-    CF chi2m, chi2a = 0.0;
+    // Per-filter chi^2 and delta_V (cuda.c:887-910); under RMSD the root of the summed chi^2 over
+    // the summed weights (cuda.c:890,901-908).
+    CF chi2m, chi2a = 0.0, SUM_w = 0.0;
     CF dv[AST_MAX_FILTERS];
     for (int m = 0; m < N_filters; m++) {
         chi2m = (CF)(sum_y2[m] - sum_y[m] * sum_y[m] / sum_w[m]);
         chi2a = chi2a + chi2m;
         dv[m] = (CF)(sum_y[m] / sum_w[m]);
+        SUM_w = (CF)((double)SUM_w + sum_w[m]);
     }
-    chi2a = chi2a / (CF)(N_data - M.n_params - N_filters);
+    if (flags & AST_RMSD)
+        chi2a = sqrt(chi2a / SUM_w);
+    else
+        chi2a = chi2a / (CF)(N_data - M.n_params - N_filters);
 
     if (flags & AST_NUDGE) {
         // Reward and punishment factors (cuda.c:912-993).

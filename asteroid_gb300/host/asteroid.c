@@ -58,6 +58,9 @@ static int default_flags(void)
 #ifdef NUDGE
     f |= AST_NUDGE;
 #endif
+#ifdef RMSD
+    f |= AST_RMSD;
+#endif
     if (f == 0) f = AST_TORQUE | AST_P_PSI; /* the README's fiducial model */
     return f;
 }
@@ -66,7 +69,7 @@ static int parse_variant(const char* s)
 {
     static const struct { const char* n; int f; } names[] = {
         {"TORQUE", AST_TORQUE}, {"BC", AST_BC}, {"BW_BALL", AST_BW_BALL}, {"P_PSI", AST_P_PSI},
-        {"INTERP", AST_INTERP}, {"ACC", AST_ACC}, {"NUDGE", AST_NUDGE}, {"LS", 0}};
+        {"INTERP", AST_INTERP}, {"ACC", AST_ACC}, {"NUDGE", AST_NUDGE}, {"RMSD", AST_RMSD}, {"LS", 0}};
     int f = 0;
     char buf[256];
     snprintf(buf, sizeof(buf), "%s", s);

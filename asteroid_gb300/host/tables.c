@@ -59,7 +59,7 @@ int ast_model_init(ast_model* m, int32_t flags, double time_step,
                    double ppsi_min_hours, double ppsi_max_hours)
 {
     if (!m) return ast_set_error(AST_E_INVALID, "ast_model_init: NULL model");
-    if (flags & ~(AST_TORQUE | AST_BC | AST_BW_BALL | AST_P_PSI | AST_INTERP | AST_ACC | AST_NUDGE))
+    if (flags & ~(AST_TORQUE | AST_BC | AST_BW_BALL | AST_P_PSI | AST_INTERP | AST_ACC | AST_NUDGE | AST_RMSD))
         return ast_set_error(AST_E_INVALID, "ast_model_init: unknown flag bits 0x%x", flags);
     if (!(time_step > 0.0))
         return ast_set_error(AST_E_INVALID, "ast_model_init: time_step must be > 0");

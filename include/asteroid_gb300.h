@@ -66,6 +66,7 @@ extern "C" {
 #define AST_INTERP   0x10  /* -DINTERP : E,S from the 3-point ephemeris at asteroid time */
 #define AST_ACC      0x20  /* -DACC    : CHI_FLOAT = double, SIZE_MIN = 1e-10 */
 #define AST_NUDGE    0x40  /* -DNUDGE  : reward for model minima near observed minima */
+#define AST_RMSD     0x80  /* -DRMSD   : chi2one returns sqrt(sum chi2_m / sum w), the RMSD */
 
 /* Property table columns (asteroid.h:115-123) */
 #define AST_P_TYPE          0

@@ -37,6 +37,8 @@ VARIANTS=(
   "bc_torque_ppsi_acc 1e-2 -DBC -DTORQUE -DP_PSI -DACC"
   "free_acc 1e-2 -DACC"
   "bc_interp_sp 1e-2 -DBC -DINTERP"
+  "rmsd_ppsi_torque_acc 1e-2 -DP_PSI -DTORQUE -DACC -DRMSD"
+  "rmsd_bc_interp_sp 1e-2 -DBC -DINTERP -DRMSD"
 )
 
 stream_source() {  # $1 = time step, $2 = 1 for the host build

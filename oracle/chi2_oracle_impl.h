@@ -247,14 +247,19 @@ ORC_CF ORC_FN(orc_chi2one)(const ast_model* md, const ast_obs_set* o, const doub
         }
     }
 
-    /* chi^2 per filter and delta_V (cuda.c:887-910). */
-    ORC_CF chi2m, chi2a = 0.0;
+    /* chi^2 per filter and delta_V (cuda.c:887-910); under RMSD the root of the summed chi^2 over
+     * the summed weights, SUM_w in CHI_FLOAT (cuda.c:890,901-908). */
+    ORC_CF chi2m, chi2a = 0.0, SUM_w = 0.0;
     for (int m = 0; m < N_filters; m++) {
         chi2m = (ORC_CF)(sum_y2[m] - sum_y[m] * sum_y[m] / sum_w[m]);
         chi2a = chi2a + chi2m;
         delta_V[m] = (ORC_CF)(sum_y[m] / sum_w[m]);
+        SUM_w = SUM_w + sum_w[m];
     }
-    chi2a = chi2a / (ORC_CF)(N_data - md->n_params - N_filters);
+    if (flags & AST_RMSD)
+        chi2a = sqrt(chi2a / SUM_w);
+    else
+        chi2a = chi2a / (ORC_CF)(N_data - md->n_params - N_filters);
 
     if (flags & AST_NUDGE) {
         /* Reward / punishment factors (cuda.c:912-993). */

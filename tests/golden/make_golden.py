@@ -36,6 +36,8 @@ VARIANTS = {
     "bc_torque_ppsi_acc": ("BC,TORQUE,P_PSI,ACC", 1e-2, 120, 1, "W", 0),
     "free_acc": ("ACC", 1e-2, 120, 1, "W", 0),
     "bc_interp_sp": ("BC,INTERP", 1e-2, 120, 2, "RV", 0),
+    "rmsd_ppsi_torque_acc": ("TORQUE,P_PSI,ACC,RMSD", 1e-2, 120, 1, "W", 0),
+    "rmsd_bc_interp_sp": ("BC,INTERP,RMSD", 1e-2, 120, 2, "RV", 0),
 }
 
 
