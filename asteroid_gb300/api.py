@@ -309,6 +309,36 @@ class Engine:
                                           dptr(s) if s is not None else None, dptr(out)), "ast_model_curve_at")
         return out
 
+    def rmsd(self, params0, dx: float, n_streams: int = 38912, samples: int = 1, seed: int = 1, call: int = 0,
+             precision: int = PREC_FP64, reopt: bool = True, spherical_k: bool = False, trace: bool = False) -> dict:
+        """One chi2_gpu_rms call (cuda.c:2148-2389): RMSD confidence intervals of params0 over
+        n_streams x samples random models (the ctx model must carry RMSD)."""
+        p0 = np.ascontiguousarray(params0, dtype=np.float64)
+        N = self.model.n_params
+        rows = int(n_streams) * int(samples)
+        cfg = capi.RmsdCfg()
+        cfg.seed = int(seed) & ((1 << 64) - 1)
+        cfg.n_streams = int(n_streams)
+        cfg.samples = int(samples)
+        cfg.precision = int(precision)
+        cfg.dx = float(dx)
+        cfg.reopt = int(bool(reopt))
+        cfg.spherical_k = int(bool(spherical_k))
+        cfg.call = int(call)
+        cfg.params0 = dptr(p0)
+        tx = np.zeros((rows, N)) if trace else None
+        tf = np.zeros(rows) if trace else None
+        if trace:
+            cfg.trace_x = dptr(tx)
+            cfg.trace_f = dptr(tf)
+        out = capi.RmsdOut()
+        check(self.lib.ast_rmsd(self.ctx, C.byref(cfg), C.byref(out)), "ast_rmsd")
+        r = {"f0": out.f0, "f1": out.f1, "n_tot": out.n_tot, "n_bad": out.n_bad,
+             "par_min": np.array(out.par_min[:N]), "par_max": np.array(out.par_max[:N]), "kernel_ms": out.kernel_ms}
+        if trace:
+            r["trace_x"], r["trace_f"] = tx, tf
+        return r
+
     def model_angles(self, params, precision: int = PREC_FP64) -> np.ndarray:
         """Euler angles [n_data, 3] along the FP64 or the mixed-precision integration."""
         p = np.ascontiguousarray(params, dtype=np.float64)

@@ -22,7 +22,7 @@ ORACLE_BUILD = ORACLE / "_build"
 
 ARCH = os.environ.get("AST_CUDA_ARCH", "sm_103a")
 GENCODE = [f"-gencode=arch=compute_{ARCH[3:]},code={ARCH}"]
-CU_SOURCES = ["csrc/engine.cu", "csrc/fit.cu", "csrc/batch.cu", "csrc/periodogram.cu"]
+CU_SOURCES = ["csrc/engine.cu", "csrc/fit.cu", "csrc/batch.cu", "csrc/periodogram.cu", "csrc/rmsd.cu"]
 C_SOURCES = ["host/tables.c", "host/read_data.c", "host/misc.c", "host/errors.c"]
 CLI_SOURCES = ["host/asteroid.c"]
 

@@ -136,6 +136,35 @@ class Periodogram(C.Structure):
 MINIMA_BINS = 10000
 
 
+class RmsdCfg(C.Structure):
+    _fields_ = [
+        ("seed", C.c_uint64),
+        ("n_streams", C.c_int64),
+        ("samples", C.c_int32),
+        ("precision", C.c_int32),
+        ("dx", C.c_double),
+        ("reopt", C.c_int32),
+        ("spherical_k", C.c_int32),
+        ("call", C.c_uint32),
+        ("reserved", C.c_int32),
+        ("params0", C.POINTER(C.c_double)),
+        ("trace_x", C.POINTER(C.c_double)),
+        ("trace_f", C.POINTER(C.c_double)),
+    ]
+
+
+class RmsdOut(C.Structure):
+    _fields_ = [
+        ("f0", C.c_double),
+        ("f1", C.c_double),
+        ("n_tot", C.c_int64),
+        ("n_bad", C.c_int64),
+        ("par_min", C.c_double * AST_MAX_PARAMS),
+        ("par_max", C.c_double * AST_MAX_PARAMS),
+        ("kernel_ms", C.c_double),
+    ]
+
+
 # Every function the header declares, with its ctypes signature.
 _P = C.c_void_p
 SIGNATURES = {
@@ -190,6 +219,7 @@ SIGNATURES = {
     "ast_batch_destroy": (None, [_P]),
     "ast_server_create": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int64, C.c_int64, C.POINTER(_P)]),
     "ast_server_set_lanes": (C.c_int, [_P, C.c_int32]),
+    "ast_rmsd": (C.c_int, [_P, C.POINTER(RmsdCfg), C.POINTER(RmsdOut)]),
     "ast_minima": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double),
                              C.POINTER(Periodogram), C.POINTER(C.c_int32)]),
     "ast_submit": (C.c_int, [_P, C.POINTER(Model), C.POINTER(ObsSet), C.POINTER(FitCfg), C.POINTER(C.c_int64)]),

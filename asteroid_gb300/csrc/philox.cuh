@@ -50,4 +50,29 @@ AST_HD float uniform01(uint64_t seed, uint64_t chain, uint32_t stage, uint32_t k
     return ((float)(u >> 8) + 0.5f) * (1.0f / 16777216.0f);
 }
 
+// Four standard normals from one Philox block (counter ctr of stream (seed, domain, stream)):
+// the Box-Muller transform (Box & Muller 1958) of the block's two pairs of uniforms, in float
+// as curand_normal is.  Host and device use their own logf / sin / cos, so the two agree to a
+// few float ulps, not bit for bit.
+AST_HD void normal4(uint64_t seed, uint64_t stream, uint32_t domain, uint32_t ctr, float z[4])
+{
+    uint32_t c[4] = {ctr, domain, (uint32_t)stream, (uint32_t)(stream >> 32)};
+    philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+#pragma unroll
+    for (int p = 0; p < 2; p++) {
+        const float u1 = ((float)(c[2 * p] >> 8) + 0.5f) * (1.0f / 16777216.0f);
+        const float u2 = ((float)(c[2 * p + 1] >> 8) + 0.5f) * (1.0f / 16777216.0f);
+        const float r = sqrtf(-2.0f * logf(u1));
+        float s, co;
+#ifdef __CUDA_ARCH__
+        sincospif(2.0f * u2, &s, &co);
+#else
+        s = sinf(6.2831853071795865f * u2);
+        co = cosf(6.2831853071795865f * u2);
+#endif
+        z[2 * p] = r * co;
+        z[2 * p + 1] = r * s;
+    }
+}
+
 }  // namespace ast

@@ -16,6 +16,9 @@
  *   -variant TORQUE,P_PSI,...   -Nblocks n   -bsize n   -time_step h   -mixed   -evals n
  *   -eph dir (directory of asteroid.eph / earth.eph / sun.eph, default ".")
  *   -Nplot n (points of the -plot model curve, default NPLOT = 20000)
+ *   -spherical_k (the -DSPHERICAL_K torque output of RMSD runs)
+ * With the RMSD variant (-variant ...,RMSD, or -DRMSD) the program computes the RMSD confidence
+ * intervals of the -m model instead of fitting (asteroid.c:643-725), with -dx and -Nstages.
  */
 #include <math.h>
 #include <stdio.h>
@@ -97,11 +100,12 @@ static void usage(void)
     printf("-Nstages number : each initial optimization stage is followed by \"number-1\" reoptimization stages\n");
     printf("-o name : output (results) file name\n");
     printf("-plot : plotting (only makes sense when -m is also used)\n");
+    printf("-dx value : maximum shift for parameters in scale-free units (0...1)  [RMSD variant]\n");
     printf("-Ppsi min max : minimum and maximum values for Ppsi period, in hours\n");
     printf("-reopt : reoptimize the model provided with -m switch\n");
     printf("-seed SEED : use the SEED number to initialize the random number generator\n");
     printf("-t : travelling reoptimization\n");
-    printf("\n GB300 engine switches: -variant TORQUE,P_PSI,... -Nblocks n -bsize n -time_step h -mixed -evals n -eph dir -Nplot n\n\n");
+    printf("\n GB300 engine switches: -variant TORQUE,P_PSI,... -Nblocks n -bsize n -time_step h -mixed -evals n -eph dir -Nplot n -spherical_k\n\n");
 }
 
 /* -plot mode (asteroid.c:834-1060, the default build): the chi^2 and delta_V of the -m model on
@@ -190,6 +194,53 @@ static int run_plot(const ast_model* m, const ast_host_data* hd, ast_ctx* ctx, c
     return rc;
 }
 
+/* -DRMSD runs (asteroid.c:643-725): repeated chi2_gpu_rms calls, each followed by one line with
+ * the fraction of bad models so far and every parameter's cumulative [min max] (stdout), and the
+ * ranges alone in the output file. */
+static int run_rmsd(ast_ctx* ctx, int N, const char* outp, const double* params, unsigned long seed, long long n_streams,
+                    int samples, float dx, int reopt, int spherical, int precision, int Ncases)
+{
+    float PAR_min[AST_MAX_PARAMS], PAR_max[AST_MAX_PARAMS];
+    for (int j = 0; j < N; j++) { PAR_min[j] = 1e30f; PAR_max[j] = -1e30f; }
+    printf("\n");
+    FILE* fp = fopen(outp, "w");
+    if (!fp) { printf("Bad output file name!\n"); return 1; }
+    long long n_tot = 0, n_bad = 0;
+    for (int loop_counter = 1;; loop_counter++) {
+        ast_rmsd_cfg cfg;
+        memset(&cfg, 0, sizeof(cfg));
+        cfg.seed = (unsigned long long)seed;
+        cfg.n_streams = n_streams;
+        cfg.samples = samples;
+        cfg.precision = precision;
+        cfg.dx = dx;
+        cfg.reopt = reopt;
+        cfg.spherical_k = spherical;
+        cfg.call = (uint32_t)(loop_counter - 1);
+        cfg.params0 = params;
+        ast_rmsd_out ro;
+        if (ast_rmsd(ctx, &cfg, &ro)) { printf("%s\n", ast_last_error()); fclose(fp); return 1; }
+        /* d_Ntot and d_Nbad accumulate over the calls (cuda.c:2348-2349). */
+        n_tot += ro.n_tot;
+        n_bad += ro.n_bad;
+        if (loop_counter == 1) printf("f0=%f, f1=%f\n\n", (double)(float)ro.f0, (double)(float)ro.f1);
+        printf("%e ", n_bad / (double)n_tot);
+        for (int j = 0; j < N; j++) {
+            if ((float)ro.par_min[j] < PAR_min[j]) PAR_min[j] = (float)ro.par_min[j];
+            if ((float)ro.par_max[j] > PAR_max[j]) PAR_max[j] = (float)ro.par_max[j];
+            printf("%13.6e %13.6e ; ", PAR_min[j], PAR_max[j]);
+            fprintf(fp, "%13.6e %13.6e ; ", PAR_min[j], PAR_max[j]);
+        }
+        printf("\n");
+        fflush(stdout);
+        fprintf(fp, "\n");
+        fflush(fp);
+        if (loop_counter == Ncases) break;
+    }
+    fclose(fp);
+    return 0;
+}
+
 int main(int argc, char** argv)
 {
     if (argc == 1) { usage(); return 0; }
@@ -200,6 +251,12 @@ int main(int argc, char** argv)
     const char *in = NULL, *outp = NULL, *eph = ".";
     int travel = 0, keep = 0, best = 0, reopt = 0, model_given = 0, plot = 0, Ncases = -1, Nstages = 1;
     int n_plot = 20000; /* NPLOT (asteroid.h:266) */
+    float dx_rand = 0.0001f; /* DX_RAND (asteroid.h:209) */
+#ifdef SPHERICAL_K
+    int spherical = 1;
+#else
+    int spherical = 0;
+#endif
     unsigned long seed = 0;
     int n_frozen = 0, n_limits = 0;
     int Fi[64], Li[64];
@@ -223,6 +280,8 @@ int main(int argc, char** argv)
         }
         else if (!strcmp(a, "-plot")) { plot = 1; j++; }
         else if (!strcmp(a, "-Nplot")) { NEED(1); n_plot = atoi(argv[j + 1]); j += 2; }
+        else if (!strcmp(a, "-dx")) { NEED(1); dx_rand = (float)atof(argv[j + 1]); j += 2; }
+        else if (!strcmp(a, "-spherical_k")) { spherical = 1; j++; }
         else if (!strcmp(a, "-t")) { travel = 1; j++; }
         else if (!strcmp(a, "-reopt")) { reopt = 1; j++; }
         else if (!strcmp(a, "-keep")) { keep = 1; j++; }
@@ -285,6 +344,15 @@ int main(int argc, char** argv)
     printf("\n*** Simplex optimization ***\n\n");
     printf("  N_threads = %lld\n", n_chains);
     if (seed == 0) seed = (unsigned long)time(NULL);
+    if (flags & AST_RMSD) {
+        /* chi2_gpu_rms reads the -m model only where -reopt uploaded it (asteroid.c:637). */
+        if (!model_given) { printf("-reopt and -plot switches require -m switch!\n"); return 1; }
+        const int rc = run_rmsd(ctx, N, outp, params, seed, n_chains, Nstages, dx_rand, reopt, spherical, precision,
+                                Ncases);
+        ast_destroy(ctx);
+        ast_free_host_data(hd);
+        return rc;
+    }
 
     double* h_f = (double*)malloc(sizeof(double) * n_blocks);
     double* h_p = (double*)malloc(sizeof(double) * n_blocks * N);

@@ -292,6 +292,46 @@ typedef struct ast_fit_out {
  * lowest chain index on ties; its delta_V is that chain's last evaluation's (cuda.c:1816-1821). */
 int ast_fit(ast_ctx* ctx, const ast_fit_cfg* cfg, ast_fit_out* out);
 
+/* ---------------------------------------------------------------- RMSD confidence intervals
+ * chi2_gpu_rms<<<N_BLOCKS, BSIZE>>> (cuda.c:2148-2389) with the host loop of asteroid.c:690-725:
+ * unconstrained confidence intervals of the -m model (Bartczak & Dudzinski 2019).  Every one of
+ * n_streams random streams draws `samples` models x = x0 + dx * N(0,1) per parameter (clamped
+ * 1e-8 inside hard limits, cuda.c:2276-2287), maps them with x2params (a rejected draw is not
+ * counted), and evaluates the RMSD; a model with RMSD below f1 = f0 + f0/sqrt(N_data - N - Nf),
+ * f0 the RMSD of the -m model, widens the [min, max] range of every parameter.  The ctx model
+ * must carry AST_RMSD.  Draws are Philox4x32-10 keyed by (seed, call, stream, draw) with
+ * Box-Muller normals: the same distribution as the reference's curand_normal, not the same
+ * numbers.  Kept from the reference: phi_M / phi_0 of a good model more than pi from the -m
+ * model's value are replaced by that value -/+ 2 pi (cuda.c:2304-2311), and under spherical_k the
+ * torque is reported as (K, theta_K, phi_K) (cuda.c:2312-2331). */
+typedef struct ast_rmsd_cfg {
+    uint64_t seed;          /* -seed */
+    int64_t  n_streams;     /* N_BLOCKS*BSIZE threads of chi2_gpu_rms */
+    int32_t  samples;       /* -Nstages: draws per stream per call */
+    int32_t  precision;     /* AST_PREC_FP64 or AST_PREC_MIXED */
+    double   dx;            /* -dx: shift scale in dimensionless units (a float in the reference) */
+    int32_t  reopt;         /* -reopt: the reopt flag x2params sees */
+    int32_t  spherical_k;   /* -DSPHERICAL_K (TORQUE models): torque as K, theta_K, phi_K */
+    uint32_t call;          /* index of this call in a sequence (each call draws new models) */
+    int32_t  reserved;
+    const double* params0;  /* the -m model [n_params] */
+    double*  trace_x;       /* optional [n_streams*samples][n_params]: every drawn point */
+    double*  trace_f;       /* optional [n_streams*samples]: its RMSD, NaN where x2params rejected it */
+} ast_rmsd_cfg;
+
+typedef struct ast_rmsd_out {
+    double  f0, f1;                     /* RMSD of the -m model and the bound (cuda.c:2225-2227) */
+    int64_t n_tot;                      /* models evaluated (d_Ntot) */
+    int64_t n_bad;                      /* of those, RMSD >= f1 or NaN (d_Nbad) */
+    double  par_min[AST_MAX_PARAMS];    /* per parameter over the good models, as float; 1e30 if none */
+    double  par_max[AST_MAX_PARAMS];    /* -1e30 if none */
+    double  kernel_ms;                  /* device time of the sampling launch */
+} ast_rmsd_out;
+
+/* One chi2_gpu_rms launch (asteroid.c:673): this call's counts and ranges (the caller
+ * accumulates them over calls as asteroid.c:698-718 does). */
+int ast_rmsd(ast_ctx* ctx, const ast_rmsd_cfg* cfg, ast_rmsd_out* out);
+
 /* The same pass split into resumable launches: chain state stays resident on the device
  * between ast_fit_step calls.  Each step lets every chain slot perform at most
  * evals_per_slot evaluations; *done becomes 1 when all stages of all chains finished. */

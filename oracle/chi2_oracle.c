@@ -13,7 +13,8 @@
  *   - one downhill-simplex chain with the reference's semantics (cuda.c:1424-1742) and the
  *     group / stage driver around it (cuda.c:1424-1823), for small cases;
  *   - an OpenMP batch evaluator, the timed CPU baseline;
- *   - minima_oracle.h: the periodogram of model minima of -plot mode (misc.c:65-276).
+ *   - minima_oracle.h: the periodogram of model minima of -plot mode (misc.c:65-276);
+ *   - rmsd_oracle.h: the RMSD confidence intervals of chi2_gpu_rms (cuda.c:2148-2389).
  * Parity status: pinned bit-for-bit against a host build of the reference's own chi2one,
  * x2params and params2x compiled from its sources (oracle/build_ref.sh, tests/golden/).
  */
@@ -184,3 +185,4 @@ float orc_uniform(uint64_t seed, uint64_t chain, uint32_t stage, uint32_t k)
 #include "nm_oracle_impl.h"
 
 #include "minima_oracle.h"
+#include "rmsd_oracle.h"
