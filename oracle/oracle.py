@@ -51,7 +51,7 @@ def load():
         lib.orc_minima.argtypes = [V, V, C.c_int, C.c_int, V, V, V, V]
         lib.orc_rmsd.restype = C.c_int
         lib.orc_rmsd.argtypes = [V, V, V, C.c_uint64, C.c_uint32, C.c_int64, C.c_int32, C.c_float, C.c_int, C.c_int,
-                                 V, V, V, V, V, V, V]
+                                 V, V, V, V, V, V, V, V]
         lib.orc_fit.restype = None
         lib.orc_fit.argtypes = [V, V, C.c_uint64, C.c_int64, C.c_int32, C.c_int32, C.c_int32, V, C.c_int64, C.c_int32,
                                 V, V, V, V, V]
@@ -111,7 +111,7 @@ def minima(t, vm, threads: int = 0):
 
 
 def rmsd(model, obs, params0, seed, call, n_streams, samples, dx, reopt=1, spherical=False, x_in=None,
-         trace=False):
+         f_in=None, trace=False):
     """RMSD confidence intervals of chi2_gpu_rms (cuda.c:2148-2389), one call.  Returns a dict with
     f0, f1, n_tot, n_bad, par_min, par_max (double) and, with trace, the drawn points and RMSDs."""
     lib = load()
@@ -126,9 +126,10 @@ def rmsd(model, obs, params0, seed, call, n_streams, samples, dx, reopt=1, spher
     tx = np.zeros((rows, N)) if trace else None
     tf = np.zeros(rows) if trace else None
     xi = None if x_in is None else np.ascontiguousarray(x_in, dtype=np.float64).reshape(rows, N)
+    fi = None if f_in is None else np.ascontiguousarray(f_in, dtype=np.float64).reshape(rows)
     lib.orc_rmsd(mp, op, p0.ctypes.data, int(seed) & ((1 << 64) - 1), int(call), int(n_streams), int(samples),
                  float(dx), int(reopt), int(bool(spherical)), None if xi is None else xi.ctypes.data,
-                 f01.ctypes.data, counts.ctypes.data, pmin.ctypes.data, pmax.ctypes.data,
+                 None if fi is None else fi.ctypes.data, f01.ctypes.data, counts.ctypes.data, pmin.ctypes.data, pmax.ctypes.data,
                  None if tx is None else tx.ctypes.data, None if tf is None else tf.ctypes.data)
     out = {"f0": f01[0], "f1": f01[1], "n_tot": int(counts[0]), "n_bad": int(counts[1]), "par_min": pmin,
            "par_max": pmax}

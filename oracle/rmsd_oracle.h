@@ -13,7 +13,8 @@
  * draw) and Box-Muller in float, with the C library's logf / sinf / cosf (the device uses its
  * own, so drawn points agree to a few float ulps).  x_in, when given, replaces the draws
  * ([n_streams*samples][N], NaN rows skipped as rejected), so a test can evaluate exactly the
- * points the device drew.
+ * points the device drew; f_in, when given, replaces the RMSDs as well, so the bookkeeping can be
+ * checked on the device's own figures.
  */
 /* Four Box-Muller normals of Philox block ctr of stream (seed, domain, stream). */
 void orc_normal4(uint64_t seed, uint64_t stream, uint32_t domain, uint32_t ctr, float z[4])
@@ -48,11 +49,12 @@ void orc_normal4(uint64_t seed, uint64_t stream, uint32_t domain, uint32_t ctr, 
 /* Returns 0; ranges as double (the device reports them rounded to float). */
 int orc_rmsd(const ast_model* md, const ast_obs_set* o, const double* params0, uint64_t seed, uint32_t call,
              int64_t n_streams, int32_t samples, float dx, int reopt, int spherical, const double* x_in,
-             double* f01, int64_t* counts, double* pmin, double* pmax, double* trace_x, double* trace_f)
+             const double* f_in, double* f01, int64_t* counts, double* pmin, double* pmax, double* trace_x,
+             double* trace_f)
 {
     if (md->flags & AST_ACC)
-        return orc_rmsd_acc(md, o, params0, seed, call, n_streams, samples, dx, reopt, spherical, x_in, f01, counts,
-                            pmin, pmax, trace_x, trace_f);
-    return orc_rmsd_sp(md, o, params0, seed, call, n_streams, samples, dx, reopt, spherical, x_in, f01, counts, pmin,
-                       pmax, trace_x, trace_f);
+        return orc_rmsd_acc(md, o, params0, seed, call, n_streams, samples, dx, reopt, spherical, x_in, f_in, f01,
+                            counts, pmin, pmax, trace_x, trace_f);
+    return orc_rmsd_sp(md, o, params0, seed, call, n_streams, samples, dx, reopt, spherical, x_in, f_in, f01, counts,
+                       pmin, pmax, trace_x, trace_f);
 }

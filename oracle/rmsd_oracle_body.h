@@ -4,8 +4,8 @@
  */
 static int RM_FN(orc_rmsd)(const ast_model* md, const ast_obs_set* o, const double* params0, uint64_t seed,
                            uint32_t call, int64_t n_streams, int32_t samples, float dx, int reopt, int spherical,
-                           const double* x_in, double* f01, int64_t* counts, double* pmin, double* pmax,
-                           double* trace_x, double* trace_f)
+                           const double* x_in, const double* f_in, double* f01, int64_t* counts, double* pmin,
+                           double* pmax, double* trace_x, double* trace_f)
 {
     const double PI_ = 3.141592653589793238;
     const ast_type_ids* T = &md->ids;
@@ -65,7 +65,7 @@ static int RM_FN(orc_rmsd)(const ast_model* md, const ast_obs_set* o, const doub
                 if (trace_f) trace_f[row] = NAN;
                 continue;
             }
-            const RM_CF f = RM_FN(orc_chi2one)(md, o, p, dv, NULL);
+            const RM_CF f = f_in ? (RM_CF)f_in[row] : RM_FN(orc_chi2one)(md, o, p, dv, NULL);
             if (trace_f) trace_f[row] = f;
             n_tot++;
             if (!(f < f1)) {

@@ -11,6 +11,7 @@ import numpy as np
 import pytest
 
 from asteroid_gb300 import api, build, capi
+from tests.test_gpu_eval import well_conditioned
 
 
 def rmsd_model(s, extra=0):
@@ -79,14 +80,20 @@ def test_gpu_rmsd_matches_oracle(gpu, oracle_mod, synth_objects, name, dx, spher
     gf, of = g["trace_f"], o["trace_f"]
     assert np.array_equal(np.isnan(gf), np.isnan(of))
     ok = ~np.isnan(of)
-    rel = np.abs(gf[ok] - of[ok]) / np.abs(of[ok])
-    assert np.max(rel) < tol, np.max(rel)
     assert g["n_tot"] == o["n_tot"] == ok.sum()
-    border = np.abs(of[ok] - o["f1"]) < 2 * tol * o["f1"]
-    assert abs(g["n_bad"] - o["n_bad"]) <= border.sum()
-    if not border.any():
-        assert np.allclose(g["par_min"], o["par_min"].astype(np.float32), rtol=1e-6, atol=1e-30)
-        assert np.allclose(g["par_max"], o["par_max"].astype(np.float32), rtol=1e-6, atol=1e-30)
+    # RMSDs agree on every well-conditioned model (the oracle's own figure moves by <= 1e-10 under
+    # one-ulp parameter changes); chaotic ones are left out as in the chi^2 parity tests.
+    P = np.array([oracle_mod.x2params(m, x, reopt=1) for x in g["trace_x"][ok]])
+    cond = well_conditioned(oracle_mod, m, s.obs, P)
+    assert cond.sum() >= 0.5 * ok.sum(), f"{cond.sum()} of {ok.sum()} well conditioned"
+    rel = np.abs(gf[ok] - of[ok]) / np.abs(of[ok])
+    assert np.max(rel[cond]) < tol, np.max(rel[cond])
+    # The bookkeeping on the device's own RMSDs: counts exact, ranges equal after the float rounding.
+    b = oracle_mod.rmsd(m, s.obs, s.params_true, seed=11, call=2, n_streams=streams, samples=samples, dx=dx,
+                        reopt=1, spherical=spherical, x_in=g["trace_x"], f_in=gf)
+    assert g["n_tot"] == b["n_tot"] and g["n_bad"] == b["n_bad"]
+    assert np.allclose(g["par_min"], b["par_min"].astype(np.float32), rtol=2.5e-7, atol=0)
+    assert np.allclose(g["par_max"], b["par_max"].astype(np.float32), rtol=2.5e-7, atol=0)
     assert 0 < g["n_bad"] < g["n_tot"]
 
 
