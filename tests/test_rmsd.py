@@ -75,7 +75,7 @@ def test_gpu_rmsd_matches_oracle(gpu, oracle_mod, synth_objects, name, dx, spher
     # The device's own points through the oracle: same RMSDs, split and ranges.
     o = oracle_mod.rmsd(m, s.obs, s.params_true, seed=11, call=2, n_streams=streams, samples=samples, dx=dx,
                         reopt=1, spherical=spherical, x_in=g["trace_x"], trace=True)
-    tol = 1e-10 if acc else 2.5e-7   # FP64 agreement; one float ulp where CHI_FLOAT is float
+    tol = 1e-9 if acc else 2.5e-7   # the FP64 tolerance against the oracle (its libm is glibc); one float ulp where CHI_FLOAT is float
     assert abs(g["f0"] - o["f0"]) <= tol * o["f0"] and abs(g["f1"] - o["f1"]) <= tol * o["f1"]
     gf, of = g["trace_f"], o["trace_f"]
     assert np.array_equal(np.isnan(gf), np.isnan(of))
