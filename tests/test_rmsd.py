@@ -97,8 +97,10 @@ def test_gpu_rmsd_matches_oracle(gpu, oracle_mod, synth_objects, name, dx, spher
     b = oracle_mod.rmsd(m, s.obs, s.params_true, seed=11, call=2, n_streams=streams, samples=samples, dx=dx,
                         reopt=1, spherical=spherical, x_in=g["trace_x"], f_in=gf)
     assert g["n_tot"] == b["n_tot"] and g["n_bad"] == b["n_bad"]
-    assert np.allclose(g["par_min"], b["par_min"].astype(np.float32), rtol=2.5e-7, atol=0)
-    assert np.allclose(g["par_max"], b["par_max"].astype(np.float32), rtol=2.5e-7, atol=0)
+    # (with CHI_FLOAT = float, x2params itself rounds to float on both sides: a few ulps apart)
+    rr = 2.5e-7 if acc else 2e-6
+    assert np.allclose(g["par_min"], b["par_min"].astype(np.float32), rtol=rr, atol=0)
+    assert np.allclose(g["par_max"], b["par_max"].astype(np.float32), rtol=rr, atol=0)
     assert 0 < g["n_bad"] < g["n_tot"]
 
 
