@@ -64,7 +64,7 @@ def test_fp64_matches_reference_kernel_on_fixtures(gpu, oracle_mod, path):
     rng = np.random.default_rng(17)
     P = [np.array(p) for p in fx["params"]]
     iL = api.param_names(m).index("L")
-    while len(P) < 64:
+    while len(P) < 160:
         p = api.x2params(m, rng.uniform(0, 1, m.n_params), reopt=0)
         if p is not None and p[iL] * m.time_step <= 0.5:
             P.append(p)
