@@ -442,6 +442,59 @@ def bench_periodogram(args, tmp, rank, world):
     print(json.dumps(line))
 
 
+def bench_rmsd(args, tmp, rank, world):
+    """RMSD confidence intervals (chi2_gpu_rms, cuda.c:2148-2389) of the config-2 object's true
+    model (TORQUE + P_PSI + INTERP + ACC + NUDGE with RMSD), dx = 1e-4: RMSD models/s of the
+    sampling kernel in both precisions, the same through ast_rmsd, and the oracle on the host."""
+    import torch
+
+    from asteroid_gb300 import api, capi, synth
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    s = synth.generate("c2", tmp)
+    m = api.make_model(s.model.flags | capi.RMSD, s.model.time_step, ppsi_hours=s.cfg.ppsi_hours)
+    streams = 38912
+    line = {"metric": "rmsd_models_per_s", "unit": "models/s", "n_gpus": 1, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "data": "synthetic", "mode": "rmsd",
+            "config": {"workload": "c2 object, RMSD variant, dx 1e-4, 38912 streams", "l2": "observations in shared memory"}}
+    with api.Engine(m, s.obs, device=local) as eng:
+        for prec, name in ((api.PREC_MIXED, "mixed"), (api.PREC_FP64, "fp64")):
+            r = eng.rmsd(s.params_true, 1e-4, n_streams=streams, samples=1, seed=1, precision=prec)
+            per_model = r["kernel_ms"] / max(r["n_tot"], 1)
+            samples = max(1, int(1500.0 / (per_model * streams)))
+            for k in range(max(args.warmup, 3) - 1):
+                eng.rmsd(s.params_true, 1e-4, n_streams=streams, samples=1, seed=2, call=k, precision=prec)
+            ms, models, wall = 0.0, 0, 0.0
+            with Clocks(local) as clk:
+                for k in range(args.steps):
+                    t0 = time.perf_counter()
+                    r = eng.rmsd(s.params_true, 1e-4, n_streams=streams, samples=samples, seed=3, call=k,
+                                 precision=prec)
+                    wall += time.perf_counter() - t0
+                    ms += r["kernel_ms"]
+                    models += r["n_tot"]
+            line[name] = {"value": models / (ms * 1e-3), "e2e": models / wall, "samples_per_stream": samples,
+                          "models": models, "ms": ms, "bad_fraction": r["n_bad"] / max(r["n_tot"], 1),
+                          "f0": r["f0"], "f1": r["f1"], "clocks": clk.summary()}
+    line["value"] = line["mixed"]["value"]
+    line["dtype"] = "mixed (double-float RK4 on the FP32 pipe); fp64 beside it"
+    line["steps"], line["warmup"] = args.steps, max(args.warmup, 3)
+    line["ms_per_step"] = line["mixed"]["ms"] / args.steps
+    line["e2e"] = {"value": line["mixed"]["e2e"], "unit": "models/s", "h2d_bytes_per_step": 8 * m.n_params,
+                   "d2h_bytes_per_step": 8 * (4 + 2 * 16)}
+    line["speedup_mixed_over_fp64"] = line["mixed"]["value"] / line["fp64"]["value"]
+    line["gpu_launches"] = 4 * args.steps
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+
+    t0 = time.perf_counter()
+    ro = O.rmsd(m, s.obs, s.params_true, seed=3, call=0, n_streams=O.max_threads(), samples=1, dx=1e-4, reopt=1)
+    cpu_s = time.perf_counter() - t0
+    line["cpu_baseline"] = {"value": ro["n_tot"] / cpu_s, "unit": "models/s", "cores": 1, "kind": "port",
+                            "sample": f"{ro['n_tot']} models on one host thread (the oracle's RMSD loop is serial)"}
+    print(json.dumps(line))
+
+
 def bench_serve(args, tmp, rank, world):
     """Config 4: Poisson arrivals of config-3 objects (1024 chains x 5000 evaluations each) at 1, 4,
     16 and 64 requests/s into one server (150 GB HBM budget); p50/p99 latency from submission to
@@ -540,10 +593,11 @@ def main():
     ap.add_argument("--budget-fp64", type=int, default=0)
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-batched", action="store_true")
-    ap.add_argument("--mode", default="fit", choices=["fit", "batch", "serve", "compare", "periodogram"],
+    ap.add_argument("--mode", default="fit", choices=["fit", "batch", "serve", "compare", "periodogram", "rmsd"],
                     help="fit: the headline line; batch: config 3 (uneven objects, one launch); "
                          "serve: config 4 (Poisson arrivals, continuous batching); compare: full fits of "
-                         "--config in both precisions at one seed; periodogram: minima() of plot mode")
+                         "--config in both precisions at one seed; periodogram: minima() of plot mode; "
+                         "rmsd: RMSD confidence intervals")
     ap.add_argument("--objects", type=int, default=512, help="batch mode: objects")
     ap.add_argument("--requests", type=int, default=8, help="serve mode: requests per arrival rate")
     ap.add_argument("--lanes", type=int, default=1, choices=[1, 4], help="serve mode: lanes per chain")
@@ -607,6 +661,8 @@ def main():
         return bench_compare(args, tmp, rank, world)
     if args.mode == "periodogram":
         return bench_periodogram(args, tmp, rank, world)
+    if args.mode == "rmsd":
+        return bench_rmsd(args, tmp, rank, world)
     s = make_workload(args, tmp)
     model, obs = s.model, s.obs
     eng = api.Engine(model, obs, device=local)
