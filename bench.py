@@ -488,7 +488,7 @@ def bench_rmsd(args, tmp, rank, world):
     import oracle as O
 
     t0 = time.perf_counter()
-    ro = O.rmsd(m, s.obs, s.params_true, seed=3, call=0, n_streams=O.max_threads(), samples=1, dx=1e-4, reopt=1)
+    ro = O.rmsd(m, s.obs, s.params_true, seed=3, call=0, n_streams=2000, samples=1, dx=1e-4, reopt=1)
     cpu_s = time.perf_counter() - t0
     line["cpu_baseline"] = {"value": ro["n_tot"] / cpu_s, "unit": "models/s", "cores": 1, "kind": "port",
                             "sample": f"{ro['n_tot']} models on one host thread (the oracle's RMSD loop is serial)"}
