@@ -208,6 +208,25 @@ def minima(t, vm, device: int = -1) -> PeriodogramResult:
                              out.n_intervals, out.kernel_ms)
 
 
+def render_frames(geo, size_pix: int = 1080, device: int = -1):
+    """ANIMATE frames [n, size_pix, size_pix, 3] (uint8) from their geometry, and the device ms."""
+    lib = capi.load()
+    g = np.ascontiguousarray(geo, dtype=np.float64).reshape(-1, capi.AST_GEO)
+    rgb = np.zeros((g.shape[0], size_pix, size_pix, 3), np.uint8)
+    ms = C.c_double(0)
+    check(lib.ast_render_frames(int(device), dptr(g), int(g.shape[0]), int(size_pix),
+                                rgb.ctypes.data_as(C.POINTER(C.c_uint8)), C.byref(ms)), "ast_render_frames")
+    return rgb, ms.value
+
+
+def write_png(path, rgb) -> None:
+    """One 8-bit RGB PNG from an [height, width, 3] uint8 array."""
+    lib = capi.load()
+    a = np.ascontiguousarray(rgb, dtype=np.uint8)
+    check(lib.ast_write_png(str(path).encode(), a.ctypes.data_as(C.POINTER(C.c_uint8)), int(a.shape[1]),
+                            int(a.shape[0])), "ast_write_png")
+
+
 def format_result(chi2, dv, params) -> str:
     """One output line in the reference's format (asteroid.c:798-811)."""
     lib = capi.load()
@@ -338,6 +357,17 @@ class Engine:
         if trace:
             r["trace_x"], r["trace_f"] = tx, tf
         return r
+
+    def model_geometry(self, params, t, e_unit=None, s_unit=None) -> np.ndarray:
+        """compute_rgb's inputs [n, 20] at increasing times t (the ANIMATE snapshots)."""
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        t = np.ascontiguousarray(t, dtype=np.float64)
+        e = None if e_unit is None else np.ascontiguousarray(e_unit, dtype=np.float64).reshape(-1, 3)
+        s = None if s_unit is None else np.ascontiguousarray(s_unit, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros((t.size, capi.AST_GEO))
+        check(self.lib.ast_model_geometry(self.ctx, dptr(p), int(t.size), dptr(t), dptr(e) if e is not None else None,
+                                          dptr(s) if s is not None else None, dptr(out)), "ast_model_geometry")
+        return out
 
     def model_angles(self, params, precision: int = PREC_FP64) -> np.ndarray:
         """Euler angles [n_data, 3] along the FP64 or the mixed-precision integration."""

@@ -22,8 +22,9 @@ ORACLE_BUILD = ORACLE / "_build"
 
 ARCH = os.environ.get("AST_CUDA_ARCH", "sm_103a")
 GENCODE = [f"-gencode=arch=compute_{ARCH[3:]},code={ARCH}"]
-CU_SOURCES = ["csrc/engine.cu", "csrc/fit.cu", "csrc/batch.cu", "csrc/periodogram.cu", "csrc/rmsd.cu"]
-C_SOURCES = ["host/tables.c", "host/read_data.c", "host/misc.c", "host/errors.c"]
+CU_SOURCES = ["csrc/engine.cu", "csrc/fit.cu", "csrc/batch.cu", "csrc/periodogram.cu", "csrc/rmsd.cu",
+              "csrc/animate.cu"]
+C_SOURCES = ["host/tables.c", "host/read_data.c", "host/misc.c", "host/errors.c", "host/png.c"]
 CLI_SOURCES = ["host/asteroid.c"]
 
 
@@ -62,6 +63,26 @@ def _headers() -> list[Path]:
     return sorted(list(PKG.glob("csrc/*.cuh")) + list(PKG.glob("host/*.h")) + list(INCLUDE.glob("*.h")))
 
 
+_ZLIB = None
+
+
+def _zlib() -> tuple[list[str], list[str]]:
+    """(-D flags, link flags) for zlib when this machine can compile and link against it; the
+    PNG writer falls back to stored deflate blocks otherwise."""
+    global _ZLIB
+    if _ZLIB is None:
+        _ZLIB = ([], [])
+        src = "#include <zlib.h>\nint main(void){uLongf n=64;unsigned char a[64],b[1]={0};return compress2(a,&n,b,1,6);}\n"
+        BUILD.mkdir(exist_ok=True)
+        for lib in ("-lz", "-l:libz.so.1"):
+            r = subprocess.run(["gcc", "-x", "c", "-", "-o", str(BUILD / "zlib_probe"), lib], input=src, text=True,
+                               stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+            if r.returncode == 0:
+                _ZLIB = (["-DAST_HAVE_ZLIB"], [lib])
+                break
+    return _ZLIB
+
+
 def build_engine(force: bool = False, ptxas_verbose: bool = False) -> Path:
     """Compile libasteroid_gb300.so (CUDA engine + C host code) and the asteroid CLI."""
     BUILD.mkdir(exist_ok=True)
@@ -84,13 +105,14 @@ def build_engine(force: bool = False, ptxas_verbose: bool = False) -> Path:
         o = BUILD / (s.stem + ".o")
         objs.append(o)
         if force or _stale(o, [s] + hdrs):
-            jobs.append(["gcc", "-O2", "-fPIC", "-std=c11", "-Wall", "-ffp-contract=off", f"-I{INCLUDE}", f"-I{PKG / 'host'}",
+            jobs.append(["gcc", "-O2", "-fPIC", "-std=c11", "-Wall", "-ffp-contract=off", *_zlib()[0], f"-I{INCLUDE}",
+                         f"-I{PKG / 'host'}",
                          "-c", str(s), "-o", str(o)])
     with ThreadPoolExecutor(max_workers=max(4, os.cpu_count() or 4)) as ex:
         list(ex.map(_run, jobs))
     lib = BUILD / "libasteroid_gb300.so"
     if force or jobs or not lib.exists():
-        _run([nvcc, *GENCODE, "-shared", "-o", str(lib), *map(str, objs), "-lcudart"])
+        _run([nvcc, *GENCODE, "-shared", "-o", str(lib), *map(str, objs), "-lcudart", *_zlib()[1]])
     cli = BUILD / "asteroid"
     cli_src = [PKG / s for s in CLI_SOURCES if (PKG / s).exists()]
     if cli_src and (force or _stale(cli, cli_src + hdrs + [lib])):

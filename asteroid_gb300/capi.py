@@ -134,6 +134,7 @@ class Periodogram(C.Structure):
 
 
 MINIMA_BINS = 10000
+AST_GEO = 20
 
 
 class RmsdCfg(C.Structure):
@@ -220,6 +221,11 @@ SIGNATURES = {
     "ast_server_create": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int64, C.c_int64, C.POINTER(_P)]),
     "ast_server_set_lanes": (C.c_int, [_P, C.c_int32]),
     "ast_rmsd": (C.c_int, [_P, C.POINTER(RmsdCfg), C.POINTER(RmsdOut)]),
+    "ast_model_geometry": (C.c_int, [_P, C.POINTER(C.c_double), C.c_int32, C.POINTER(C.c_double),
+                                     C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "ast_render_frames": (C.c_int, [C.c_int32, C.POINTER(C.c_double), C.c_int32, C.c_int32, C.POINTER(C.c_uint8),
+                                    C.POINTER(C.c_double)]),
+    "ast_write_png": (C.c_int, [C.c_char_p, C.POINTER(C.c_uint8), C.c_int32, C.c_int32]),
     "ast_minima": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double),
                              C.POINTER(Periodogram), C.POINTER(C.c_int32)]),
     "ast_submit": (C.c_int, [_P, C.POINTER(Model), C.POINTER(ObsSet), C.POINTER(FitCfg), C.POINTER(C.c_int64)]),

@@ -1,0 +1,180 @@
+// animate.cu -- frames of the ANIMATE build (compute_rgb, cuda.c:2394-2540 of the reference).
+//
+// The reference runs chi2_plot<<<ceil(SIZE_PIX^2 / BSIZE), BSIZE>>> in which every thread
+// integrates the whole model over the plot grid (one RK4 recursion per pixel) and, at each
+// snapshot, shades its own pixel: four lines of sight through the pixel's corners intersected with
+// the triaxial ellipsoid, Lambert-like shading between terminator, shadow and sunlit colours, a
+// red spot around the end of the b axis.  Here the recursion runs once (ast_model_geometry: one
+// thread, the fit's FP64 evaluation) and render_kernel shades every pixel of every frame from
+// that geometry: one thread per pixel, frames on the grid's y dimension, the frame's 20 doubles in
+// shared memory.  The arithmetic is the reference's, in FP64, with every rounding explicit (no
+// contracted multiply-adds) so that the CPU restatement reproduces each byte.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+#include <algorithm>
+
+#include "asteroid_gb300.h"
+#include "dfloat.cuh"
+#include "engine.cuh"
+
+namespace ast {
+namespace {
+
+constexpr int kRenderTpb = 256;
+// Colours (asteroid.h:300-313): deepest shadow, terminator, brightest sunlit element.
+constexpr float kSminR = 6, kSminG = 8, kSminB = 10;
+constexpr float kSmaxR = 30, kSmaxG = 41, kSmaxB = 53;
+constexpr float kImaxR = 255, kImaxG = 191, kImaxB = 144;
+constexpr float kSpotRad = 0.04f;  // SPOT_RAD (asteroid.h:315), a float: its square is rounded to float
+
+#define M_(a, b) DD_MUL(a, b)
+#define A_(a, b) DD_ADD(a, b)
+#define S_(a, b) DD_SUB(a, b)
+
+__global__ void __launch_bounds__(kRenderTpb) render_kernel(const double* __restrict__ geo, int n_frames, int S,
+                                                            uint8_t* __restrict__ rgb)
+{
+    __shared__ double g[kAstGeo];
+    __shared__ double Z1x, Z1z, Y1x, Y1y, Y1z;
+    const int f = blockIdx.y;
+    if (threadIdx.x < kAstGeo) g[threadIdx.x] = geo[(int64_t)kAstGeo * f + threadIdx.x];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        // Image axes: X1 toward the observer (E), Z1 = [E x y], Y1 = [Z1 x X1] (cuda.c:2418-2427).
+        const double Ex = g[2], Ey = g[3], Ez = g[4];
+        const double scale = 1.0 / sqrt(A_(M_(Ex, Ex), M_(Ez, Ez)));
+        Z1x = M_(-Ez, scale);
+        Z1z = M_(Ex, scale);
+        Y1x = M_(M_(-Ex, Ey), scale);
+        Y1y = M_(A_(M_(Ex, Ex), M_(Ez, Ez)), scale);
+        Y1z = M_(M_(-Ey, Ez), scale);
+    }
+    __syncthreads();
+    const int id = blockIdx.x * kRenderTpb + threadIdx.x;
+    if (id >= S * S) return;
+    const int iz = id / S, iy = id % S;
+    const double b = g[0], c = g[1];
+    const double Epb = g[5], Epc = g[6], Epa = g[7], Spb = g[8], Spc = g[9], Spa = g[10];
+    const double bb = M_(b, b), cc = M_(c, c);
+    float br[3] = {0.f, 0.f, 0.f};
+    for (int jz = 0; jz < 2; jz++) {
+        const double z1 = 2.4 * (double)(iz - S / 2 + jz) / (double)S;
+        for (int jy = 0; jy < 2; jy++) {
+            const double y1 = 2.4 * (double)(iy - S / 2 + jy) / (double)S;
+            const double p_x = A_(M_(y1, Y1x), M_(z1, Z1x));
+            const double p_y = A_(M_(y1, Y1y), M_(z1, 0.0));
+            const double p_z = A_(M_(y1, Y1z), M_(z1, Z1z));
+            const double p_b = A_(A_(M_(g[11], p_x), M_(g[12], p_y)), M_(g[13], p_z));
+            const double p_c = A_(A_(M_(g[14], p_x), M_(g[15], p_y)), M_(g[16], p_z));
+            const double p_a = A_(A_(M_(g[17], p_x), M_(g[18], p_y)), M_(g[19], p_z));
+            // Line of sight p + lambda E' against the ellipsoid (b, c, 1) (cuda.c:2453-2460).
+            const double A = A_(A_(M_(Epb, Epb) / bb, M_(Epc, Epc) / cc), M_(Epa, Epa));
+            const double B = M_(2.0, A_(A_(M_(p_b, Epb) / bb, M_(p_c, Epc) / cc), M_(p_a, Epa)));
+            const double C = S_(A_(A_(M_(p_b, p_b) / bb, M_(p_c, p_c) / cc), M_(p_a, p_a)), 1.0);
+            const double D = S_(M_(B, B), M_(M_(4.0, A), C));
+            if (D >= 0.0) {
+                const double sD = sqrt(D);
+                double lambda = S_(-B, sD) / M_(2.0, A);
+                const double lambda1 = A_(-B, sD) / M_(2.0, A);
+                if (lambda1 > lambda) lambda = lambda1;
+                const double ri_b = A_(p_b, M_(lambda, Epb));
+                const double ri_c = A_(p_c, M_(lambda, Epc));
+                const double ri_a = A_(p_a, M_(lambda, Epa));
+                const int red_spot = (A_(M_(ri_c, ri_c), M_(ri_a, ri_a)) < (double)(kSpotRad * kSpotRad) && ri_b > 0.0) ? 1 : 0;
+                double ni_b = ri_b / bb, ni_c = ri_c / cc, ni_a = ri_a;
+                const double scale = 1.0 / sqrt(A_(A_(M_(ni_b, ni_b), M_(ni_c, ni_c)), M_(ni_a, ni_a)));
+                ni_b = M_(ni_b, scale);
+                ni_c = M_(ni_c, scale);
+                ni_a = M_(ni_a, scale);
+                const double I = A_(A_(M_(ni_b, Spb), M_(ni_c, Spc)), M_(ni_a, Spa));
+                // float + float + double*float, rounded back to float (cuda.c:2500-2525).
+                if (I >= 0.0) {
+                    br[0] = (float)A_((double)(br[0] + kSmaxR), M_(I, (double)(kImaxR - kSmaxR)));
+                    if (red_spot == 0) {
+                        br[1] = (float)A_((double)(br[1] + kSmaxG), M_(I, (double)(kImaxG - kSmaxG)));
+                        br[2] = (float)A_((double)(br[2] + kSmaxB), M_(I, (double)(kImaxB - kSmaxB)));
+                    }
+                } else {
+                    br[0] = (float)A_((double)(br[0] + kSmaxR), M_(I, (double)(kSmaxR - kSminR)));
+                    if (red_spot == 0) {
+                        br[1] = (float)A_((double)(br[1] + kSmaxG), M_(I, (double)(kSmaxG - kSminG)));
+                        // The reference adds to br[1] here, not br[2] (cuda.c:2523).
+                        br[2] = (float)A_((double)(br[1] + kSmaxB), M_(I, (double)(kSmaxB - kSminB)));
+                    }
+                }
+            }
+        }
+    }
+    uint8_t* out = rgb + 3 * ((int64_t)iy + (int64_t)S * ((int64_t)iz + (int64_t)S * f));
+#pragma unroll
+    for (int ic = 0; ic < 3; ic++) {
+        int v = (int)((double)br[ic] / 4.0);
+        v = v > 255 ? 255 : (v < 0 ? 0 : v);
+        out[ic] = (uint8_t)v;
+    }
+}
+
+#undef M_
+#undef A_
+#undef S_
+
+struct RenderScratch {
+    double* geo = nullptr;
+    uint8_t* rgb = nullptr;
+    cudaStream_t s = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    ~RenderScratch()
+    {
+        cudaFree(geo);
+        cudaFree(rgb);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        if (s) cudaStreamDestroy(s);
+    }
+};
+
+}  // namespace
+}  // namespace ast
+
+using namespace ast;
+
+extern "C" int ast_render_frames(int32_t device, const double* geo, int32_t n_frames, int32_t size_pix, uint8_t* rgb,
+                                 double* kernel_ms)
+{
+    if (!geo || !rgb || n_frames < 0 || size_pix < 2 || size_pix > 8192 || (size_pix & 1))
+        return ast_set_error(AST_E_INVALID, "ast_render_frames: bad argument");
+    if (kernel_ms) *kernel_ms = 0;
+    if (n_frames == 0) return AST_OK;
+    int rc = set_device(device);
+    if (rc) return rc;
+    const int64_t frame_bytes = 3ll * size_pix * size_pix;
+    // Frames per launch: at most 2 GB of pixels on the device at once (the reference uses dNPLOT).
+    const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(n_frames, (2ll << 30) / frame_bytes));
+    RenderScratch d;
+    if (cudaMalloc(&d.geo, sizeof(double) * kAstGeo * chunk) != cudaSuccess ||
+        cudaMalloc(&d.rgb, (size_t)(frame_bytes * chunk)) != cudaSuccess) {
+        cudaGetLastError();
+        return ast_set_error(AST_E_NOMEM, "ast_render_frames: cudaMalloc failed");
+    }
+    AST_CUDA(cudaStreamCreateWithFlags(&d.s, cudaStreamNonBlocking));
+    AST_CUDA(cudaEventCreate(&d.e0));
+    AST_CUDA(cudaEventCreate(&d.e1));
+    const unsigned blocks = (unsigned)((size_pix * size_pix + kRenderTpb - 1) / kRenderTpb);
+    double total = 0;
+    for (int64_t f0 = 0; f0 < n_frames; f0 += chunk) {
+        const int64_t nf = std::min<int64_t>(chunk, n_frames - f0);
+        AST_CUDA(cudaMemcpyAsync(d.geo, geo + kAstGeo * f0, sizeof(double) * kAstGeo * nf, cudaMemcpyHostToDevice, d.s));
+        AST_CUDA(cudaEventRecord(d.e0, d.s));
+        render_kernel<<<dim3(blocks, (unsigned)nf), kRenderTpb, 0, d.s>>>(d.geo, (int)nf, size_pix, d.rgb);
+        AST_CUDA(cudaGetLastError());
+        AST_CUDA(cudaEventRecord(d.e1, d.s));
+        AST_CUDA(cudaMemcpyAsync(rgb + frame_bytes * f0, d.rgb, (size_t)(frame_bytes * nf), cudaMemcpyDeviceToHost, d.s));
+        AST_CUDA(cudaStreamSynchronize(d.s));
+        float ms = 0;
+        AST_CUDA(cudaEventElapsedTime(&ms, d.e0, d.e1));
+        total += ms;
+    }
+    if (kernel_ms) *kernel_ms = total;
+    return AST_OK;
+}

@@ -146,9 +146,10 @@ __global__ void __launch_bounds__(128) eval_kernel(DevModel M, const void* g_obs
     bulk_drain(&bar, staged || !use_smem);
 }
 
-// Model magnitudes of one parameter vector at every observation (single thread: the RK4
-// recursion is sequential in time).
-__global__ void model_curve_kernel(DevModel M, const void* g_obs, ObsLayout L, const double* params, double* vmod)
+// Model magnitudes (and, with geo, the renderer's geometry) of one parameter vector at every
+// observation (single thread: the RK4 recursion is sequential in time).
+__global__ void model_curve_kernel(DevModel M, const void* g_obs, ObsLayout L, const double* params, double* vmod,
+                                   double* geo = nullptr)
 {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
     const ObsView o = L.view(g_obs, M.n_data);
@@ -157,7 +158,7 @@ __global__ void model_curve_kernel(DevModel M, const void* g_obs, ObsLayout L, c
     double d[AST_MAX_FILTERS];
     DevModel M2 = M;
     M2.flags &= ~AST_NUDGE;  // the curve is the brightness model alone
-    chi2_fp64<double>(M2, o, p, d, vmod);
+    chi2_fp64<double>(M2, o, p, d, vmod, nullptr, geo);
 }
 
 // Euler angles at every observation along the FP64 or the mixed-precision integration.
@@ -411,10 +412,11 @@ extern "C" int ast_model_curve(ast_ctx* c, const double* params, double* vmod)
     return AST_OK;
 }
 
-extern "C" int ast_model_curve_at(ast_ctx* c, const double* params, int32_t n, const double* t,
-                                  const double* e_unit, const double* s_unit, double* vmod)
+// The model at n other times: magnitudes (vmod) and / or the renderer's geometry (geo).
+static int curve_at(ast_ctx* c, const double* params, int32_t n, const double* t, const double* e_unit,
+                    const double* s_unit, double* vmod, double* geo)
 {
-    if (!c || !params || !t || !vmod || n < 2) return ast_set_error(AST_E_INVALID, "ast_model_curve_at: bad argument");
+    if (!c || !params || !t || (!vmod && !geo) || n < 2) return ast_set_error(AST_E_INVALID, "ast_model_curve_at: bad argument");
     const bool interp = (c->model.flags & AST_INTERP) != 0;
     if (!interp && (!e_unit || !s_unit)) return ast_set_error(AST_E_INVALID, "ast_model_curve_at: E and S needed");
     for (int32_t i = 1; i < n; i++)
@@ -446,21 +448,38 @@ extern "C" int ast_model_curve_at(ast_ctx* c, const double* params, int32_t n, c
         void* blk = nullptr;
         double* p = nullptr;
         double* v = nullptr;
-        ~Scratch() { cudaFree(blk); cudaFree(p); cudaFree(v); }
+        double* g = nullptr;
+        ~Scratch() { cudaFree(blk); cudaFree(p); cudaFree(v); cudaFree(g); }
     } d;
     if (cudaMalloc(&d.blk, (size_t)L.bytes) != cudaSuccess || cudaMalloc(&d.p, sizeof(double) * AST_MAX_PARAMS) != cudaSuccess ||
-        cudaMalloc(&d.v, sizeof(double) * n) != cudaSuccess) {
+        cudaMalloc(&d.v, sizeof(double) * n) != cudaSuccess ||
+        (geo && cudaMalloc(&d.g, sizeof(double) * kAstGeo * n) != cudaSuccess)) {
         cudaGetLastError();
         return ast_set_error(AST_E_NOMEM, "ast_model_curve_at: cudaMalloc failed");
     }
     AST_CUDA(cudaMemcpyAsync(d.blk, img.data(), img.size(), cudaMemcpyHostToDevice, c->stream));
     AST_CUDA(cudaMemcpyAsync(d.p, params, sizeof(double) * c->model.n_params, cudaMemcpyHostToDevice, c->stream));
     if ((rc = launch_prep(dm, (char*)d.blk, L, n, c->stream))) return rc;
-    model_curve_kernel<<<1, 32, 0, c->stream>>>(dm, d.blk, L, d.p, d.v);
+    model_curve_kernel<<<1, 32, 0, c->stream>>>(dm, d.blk, L, d.p, d.v, d.g);
     AST_CUDA(cudaGetLastError());
-    AST_CUDA(cudaMemcpyAsync(vmod, d.v, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    if (vmod) AST_CUDA(cudaMemcpyAsync(vmod, d.v, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    if (geo) AST_CUDA(cudaMemcpyAsync(geo, d.g, sizeof(double) * kAstGeo * n, cudaMemcpyDeviceToHost, c->stream));
     AST_CUDA(cudaStreamSynchronize(c->stream));
     return AST_OK;
+}
+
+extern "C" int ast_model_curve_at(ast_ctx* c, const double* params, int32_t n, const double* t,
+                                  const double* e_unit, const double* s_unit, double* vmod)
+{
+    if (!vmod) return ast_set_error(AST_E_INVALID, "ast_model_curve_at: NULL vmod");
+    return curve_at(c, params, n, t, e_unit, s_unit, vmod, nullptr);
+}
+
+extern "C" int ast_model_geometry(ast_ctx* c, const double* params, int32_t n, const double* t,
+                                  const double* e_unit, const double* s_unit, double* geo)
+{
+    if (!geo) return ast_set_error(AST_E_INVALID, "ast_model_geometry: NULL geo");
+    return curve_at(c, params, n, t, e_unit, s_unit, nullptr, geo);
 }
 
 extern "C" int ast_model_angles(ast_ctx* c, int32_t precision, const double* params, double* angles)

@@ -350,10 +350,27 @@ struct Geometry {
 // "more than M_MAX minima" exit returns 1e30 and leaves it, as the reference does).
 // vmod_out, when non-null, receives the model magnitude of every observation (the reference's
 // Nplot > 0 mode, cuda.c:699-704, without the delta_V shift); ang_out the Euler angles
-// (phi, theta, psi) at every observation.
+// (phi, theta, psi) at every observation; geo_out the kAstGeo inputs of the ANIMATE renderer
+// at every observation (compute_rgb's arguments, cuda.c:576-586).
+constexpr int kAstGeo = 20;
+
+__device__ __forceinline__ void write_geo(double* g, double b, double c, double Ex, double Ey, double Ez, double Epb,
+                                          double Epc, double Epa, double Spb, double Spc, double Spa, double bx,
+                                          double by, double bz, double cx, double cy, double cz, double ax, double ay,
+                                          double az)
+{
+    g[0] = b; g[1] = c;
+    g[2] = Ex; g[3] = Ey; g[4] = Ez;
+    g[5] = Epb; g[6] = Epc; g[7] = Epa;
+    g[8] = Spb; g[9] = Spc; g[10] = Spa;
+    g[11] = bx; g[12] = by; g[13] = bz;
+    g[14] = cx; g[15] = cy; g[16] = cz;
+    g[17] = ax; g[18] = ay; g[19] = az;
+}
+
 template <class CF>
 __device__ CF chi2_fp64(const DevModel& M, const ObsView& o, const double* params, CF* delta_V,
-                        double* vmod_out = nullptr, double* ang_out = nullptr)
+                        double* vmod_out = nullptr, double* ang_out = nullptr, double* geo_out = nullptr)
 {
     const int flags = M.flags;
     const ast_type_ids& T = M.t;
@@ -486,6 +503,11 @@ __device__ CF chi2_fp64(const DevModel& M, const ObsView& o, const double* param
             a_y = a_y * cos_thR + p_y * sin_thR;
             a_z = a_z * cos_thR + p_z * sin_thR;
             const double Ep_a = a_x * E_x1 + a_y * E_y1 + a_z * E_z1;
+            if (geo_out)
+                write_geo(geo_out + (int64_t)kAstGeo * i, bt, ct, E_x1, E_y1, E_z1, b_x * E_x1 + b_y * E_y1 + b_z * E_z1,
+                          c_x * E_x1 + c_y * E_y1 + c_z * E_z1, Ep_a, b_x * S_x1 + b_y * S_y1 + b_z * S_z1,
+                          c_x * S_x1 + c_y * S_y1 + c_z * S_z1, a_x * S_x1 + a_y * S_y1 + a_z * S_z1, b_x, b_y, b_z,
+                          c_x, c_y, c_z, a_x, a_y, a_z);
             const double cos_zeta = Ep_a;
             Vmod = -2.5 * log10(0.5 * (kappa * (1 + cos_zeta) + 0.5 * (1 - cos_zeta)));
         } else {
@@ -497,6 +519,9 @@ __device__ CF chi2_fp64(const DevModel& M, const ObsView& o, const double* param
             const double Sp_a = a_x * S_x1 + a_y * S_y1 + a_z * S_z1;
             // Lommel-Seeliger ellipsoid, Muinonen & Lumme (2015) eqs. 10-14 (cuda.c:664-689).
             const double b = b_ph, c = c_ph;
+            if (geo_out)
+                write_geo(geo_out + (int64_t)kAstGeo * i, b, c, E_x1, E_y1, E_z1, Ep_b, Ep_c, Ep_a, Sp_b, Sp_c, Sp_a,
+                          b_x, b_y, b_z, c_x, c_y, c_z, a_x, a_y, a_z);
             const double scalar_Sun = sqrt(Sp_b * Sp_b / (b * b) + Sp_c * Sp_c / (c * c) + Sp_a * Sp_a);
             const double scalar_Earth = sqrt(Ep_b * Ep_b / (b * b) + Ep_c * Ep_c / (c * c) + Ep_a * Ep_a);
             const double cos_alpha_p = (Sp_b * Ep_b / (b * b) + Sp_c * Ep_c / (c * c) + Sp_a * Ep_a) / (scalar_Sun * scalar_Earth);

@@ -17,6 +17,8 @@
  *   -eph dir (directory of asteroid.eph / earth.eph / sun.eph, default ".")
  *   -Nplot n (points of the -plot model curve, default NPLOT = 20000)
  *   -spherical_k (the -DSPHERICAL_K torque output of RMSD runs)
+ *   -animate (the -DANIMATE build: -plot renders image_%05d.png frames, with -i1 / -i2, NPLOT 15440)
+ *   -size_pix n (frame size, default SIZE_PIX = 1080)
  * With the RMSD variant (-variant ...,RMSD, or -DRMSD) the program computes the RMSD confidence
  * intervals of the -m model instead of fitting (asteroid.c:643-725), with -dx and -Nstages.
  */
@@ -92,6 +94,8 @@ static void usage(void)
     printf("-best : only keep the best result\n");
     printf("-f type_constant value: forces the parameter with the type_constant to be frozen during optimization at \"value\" \n");
     printf("-i name : input (data) file name\n");
+    printf("-i1 index : index of the first snapshot  [-animate]\n");
+    printf("-i2 index : index of the last snapshot minus one  [-animate]\n");
     printf("-keep : keep all intermediate results, not just the best ones\n");
     printf("-l type_constant limit1 limit2 : specify range for the parameter type_constant\n");
     printf("-m param1 param2 ... paramN : input model parameters, for plotting and re-optimization\n");
@@ -105,7 +109,8 @@ static void usage(void)
     printf("-reopt : reoptimize the model provided with -m switch\n");
     printf("-seed SEED : use the SEED number to initialize the random number generator\n");
     printf("-t : travelling reoptimization\n");
-    printf("\n GB300 engine switches: -variant TORQUE,P_PSI,... -Nblocks n -bsize n -time_step h -mixed -evals n -eph dir -Nplot n -spherical_k\n\n");
+    printf("\n GB300 engine switches: -variant TORQUE,P_PSI,... -Nblocks n -bsize n -time_step h -mixed -evals n -eph dir -Nplot n -spherical_k\n"
+           "   -animate -size_pix n\n\n");
 }
 
 /* -plot mode (asteroid.c:834-1060, the default build): the chi^2 and delta_V of the -m model on
@@ -194,6 +199,48 @@ static int run_plot(const ast_model* m, const ast_host_data* hd, ast_ctx* ctx, c
     return rc;
 }
 
+/* -plot under ANIMATE (asteroid.c:863-878): the frames of snapshots i1 .. i2-1 in steps of
+ * dNPLOT = 1500, each step ending at min(start + 1500, NPLOT) as the reference's loop does, written
+ * as image_%05d.png (misc.c:372-460).  Rendered in groups of at most 64 frames. */
+static int run_animate(const ast_host_data* hd, ast_ctx* ctx, const double* params, int interp, int n_plot, int i1,
+                       int i2, int size_pix)
+{
+    printf("\n*** Plotting ***\n\n");
+    if (i1 < 0 || i2 > n_plot || i1 >= i2) { printf("Bad arguments!\n"); return 1; }
+    double* t = (double*)malloc(sizeof(double) * n_plot);
+    double* e = (double*)malloc(sizeof(double) * 3 * n_plot);
+    double* sv = (double*)malloc(sizeof(double) * 3 * n_plot);
+    double* geo = (double*)malloc(sizeof(double) * AST_GEO * n_plot);
+    const int group = 64;
+    uint8_t* rgb = (uint8_t*)malloc((size_t)3 * size_pix * size_pix * group);
+    int rc = (!t || !e || !sv || !geo || !rgb) ? 1 : 0;
+    if (!rc && (ast_plot_grid(hd, interp, n_plot, t, e, sv) || ast_model_geometry(ctx, params, n_plot, t, e, sv, geo))) {
+        printf("%s\n", ast_last_error());
+        rc = 1;
+    }
+    for (int h_i1 = i1; !rc && h_i1 < i2; h_i1 += 1500) {
+        const int h_i2 = h_i1 + 1500 > n_plot ? n_plot : h_i1 + 1500;
+        for (int f0 = h_i1; !rc && f0 < h_i2; f0 += group) {
+            const int nf = h_i2 - f0 < group ? h_i2 - f0 : group;
+            if (ast_render_frames(-1, geo + (size_t)AST_GEO * f0, nf, size_pix, rgb, NULL)) {
+                printf("%s\n", ast_last_error());
+                rc = 1;
+                break;
+            }
+            for (int k = 0; k < nf && !rc; k++) {
+                char name[64];
+                snprintf(name, sizeof(name), "image_%05d.png", f0 + k);
+                if (ast_write_png(name, rgb + (size_t)3 * size_pix * size_pix * k, size_pix, size_pix)) {
+                    fprintf(stderr, "%s\n", ast_last_error());
+                    rc = 1;
+                }
+            }
+        }
+    }
+    free(t); free(e); free(sv); free(geo); free(rgb);
+    return rc;
+}
+
 /* -DRMSD runs (asteroid.c:643-725): repeated chi2_gpu_rms calls, each followed by one line with
  * the fraction of bad models so far and every parameter's cumulative [min max] (stdout), and the
  * ranges alone in the output file. */
@@ -252,6 +299,12 @@ int main(int argc, char** argv)
     int travel = 0, keep = 0, best = 0, reopt = 0, model_given = 0, plot = 0, Ncases = -1, Nstages = 1;
     int n_plot = 20000; /* NPLOT (asteroid.h:266) */
     float dx_rand = 0.0001f; /* DX_RAND (asteroid.h:209) */
+#ifdef ANIMATE
+    int animate = 1;
+#else
+    int animate = 0;
+#endif
+    int i1_input = 0, i2_input = -1, size_pix = AST_SIZE_PIX, nplot_given = 0;
 #ifdef SPHERICAL_K
     int spherical = 1;
 #else
@@ -279,7 +332,11 @@ int main(int argc, char** argv)
             model_given = 1;
         }
         else if (!strcmp(a, "-plot")) { plot = 1; j++; }
-        else if (!strcmp(a, "-Nplot")) { NEED(1); n_plot = atoi(argv[j + 1]); j += 2; }
+        else if (!strcmp(a, "-Nplot")) { NEED(1); n_plot = atoi(argv[j + 1]); nplot_given = 1; j += 2; }
+        else if (!strcmp(a, "-animate")) { animate = 1; j++; }
+        else if (!strcmp(a, "-i1")) { NEED(1); i1_input = atoi(argv[j + 1]); j += 2; }
+        else if (!strcmp(a, "-i2")) { NEED(1); i2_input = atoi(argv[j + 1]); j += 2; }
+        else if (!strcmp(a, "-size_pix")) { NEED(1); size_pix = atoi(argv[j + 1]); j += 2; }
         else if (!strcmp(a, "-dx")) { NEED(1); dx_rand = (float)atof(argv[j + 1]); j += 2; }
         else if (!strcmp(a, "-spherical_k")) { spherical = 1; j++; }
         else if (!strcmp(a, "-t")) { travel = 1; j++; }
@@ -304,6 +361,8 @@ int main(int argc, char** argv)
     if (!in) { printf("-i parameter is missing!\n"); return 1; }
     if ((reopt || plot) && !model_given) { printf("-reopt and -plot switches require -m switch!\n"); return 1; }
     if (!reopt && !plot && model_given) { printf("-m can only be used together with -reopt or -plot switches!\n"); return 1; }
+    if (animate && !nplot_given) n_plot = AST_NPLOT_ANIMATE;
+    if (i2_input < 0) i2_input = n_plot;
     if (plot && n_plot < 2) { printf("Bad arguments!\n"); return 1; }
 
     ast_model model;
@@ -332,6 +391,12 @@ int main(int argc, char** argv)
     }
     ast_ctx* ctx = NULL;
     if (ast_prepare(&model, &hd->obs, -1, &ctx)) { printf("%s\n", ast_last_error()); return 1; }
+    if (plot && animate) {
+        const int rc = run_animate(hd, ctx, params, (flags & AST_INTERP) != 0, n_plot, i1_input, i2_input, size_pix);
+        ast_destroy(ctx);
+        ast_free_host_data(hd);
+        return rc;
+    }
     if (plot) {
         const int rc = run_plot(&model, hd, ctx, params, (flags & AST_INTERP) != 0, n_plot);
         ast_destroy(ctx);

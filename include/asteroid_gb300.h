@@ -227,6 +227,31 @@ int ast_model_curve(ast_ctx* ctx, const double* params, double* vmod);
 int ast_model_curve_at(ast_ctx* ctx, const double* params, int32_t n, const double* t, const double* e_unit,
                        const double* s_unit, double* vmod);
 
+/* ---------------------------------------------------------------- ANIMATE frames
+ * The -DANIMATE build renders the asteroid as seen from Earth at every plot-grid time
+ * (chi2one's compute_rgb call, cuda.c:576-586; compute_rgb cuda.c:2394-2540) and writes
+ * image_%05d.png files (write_PNGs, misc.c:372-460).  Here that is three calls: the geometry of
+ * every snapshot, the frames, and a PNG writer. */
+#define AST_GEO       20    /* doubles per snapshot, see ast_model_geometry */
+#define AST_SIZE_PIX  1080  /* SIZE_PIX (asteroid.h:259) */
+#define AST_NPLOT_ANIMATE 15440 /* NPLOT of the ANIMATE build (asteroid.h:264) */
+
+/* Geometry at n increasing times (as ast_model_curve_at), geo[AST_GEO*i + k]: b, c (the
+ * brightness ellipsoid's axes), E (unit, inertial), E and S in the body frame (b, c, a
+ * components), and the body axes b, c, a in inertial coordinates. */
+int ast_model_geometry(ast_ctx* ctx, const double* params, int32_t n, const double* t, const double* e_unit,
+                       const double* s_unit, double* geo);
+
+/* compute_rgb for n_frames snapshots on CUDA device `device` (-1: current): rgb receives
+ * n_frames x size_pix x size_pix x 3 bytes, rgb[ic + 3*(x + size_pix*(y + size_pix*f))], the
+ * reference's d_rgb layout (row y = the image's z1 axis).  size_pix even, <= 8192.  kernel_ms
+ * (optional) receives the device time of the rendering. */
+int ast_render_frames(int32_t device, const double* geo, int32_t n_frames, int32_t size_pix, uint8_t* rgb,
+                      double* kernel_ms);
+
+/* One 8-bit RGB PNG (write_PNGs' per-snapshot file; colour type 2, no interlace). */
+int ast_write_png(const char* path, const uint8_t* rgb, int32_t width, int32_t height);
+
 /* Euler angles (phi, theta, psi) at every observation, angles[3*i + k], as integrated by the
  * FP64 path or by the mixed path (double-float state, reduced to [-pi, pi] at each
  * observation): the phase drift of the mixed path.  No reference counterpart. */

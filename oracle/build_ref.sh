@@ -10,6 +10,8 @@
 #                        oracle/ref_gpu_loader.cpp to check the CUDA path at 1e-12.
 #   libref_minima.so     host build of minima() (misc.c:65-276, default macros) with
 #                        oracle/ref_harness_minima.cu; pins the periodogram oracle.
+#   ref_animate.cubin    device build (sm_100) of cuda.c with -DANIMATE plus
+#                        oracle/ref_harness_animate.cu: the reference's compute_rgb on the GPU.
 #
 # The reference's asteroid.h and cuda.c are streamed through sed into nvcc's standard input:
 # the four device functions become __host__ __device__ (host build only), N_FILTERS becomes 8
@@ -67,7 +69,14 @@ if [[ -f "$REF/misc.c" && ( "${1:-all}" == "all" || "${1:-all}" == "host" || "${
            -o "$OUT/libref_minima.so" - ) &
     pids+=($!)
 fi
-[[ "${1:-all}" == "minima" ]] && VARIANTS=()
+if [[ "${1:-all}" == "all" || "${1:-all}" == "cubin" || "${1:-all}" == "animate" ]]; then
+    ( { sed -e 's/^const int N_FILTERS = 1;/const int N_FILTERS = 8;/' -e 's|^ *#include <png.h>||' "$REF/asteroid.h"
+        sed -e 's/^#include "asteroid.h"//' "$REF/cuda.c"
+        cat "$here/ref_harness_animate.cu"; } |
+      nvcc -x cu -cubin -arch=sm_100 -O3 -DMAIN -DANIMATE -I"$REF" -w -o "$OUT/ref_animate.cubin" - ) &
+    pids+=($!)
+fi
+[[ "${1:-all}" == "minima" || "${1:-all}" == "animate" ]] && VARIANTS=()
 for v in "${VARIANTS[@]}"; do
     read -r name ts macros <<<"$v"
     if [[ "${1:-all}" == "all" || "${1:-all}" == "host" ]]; then

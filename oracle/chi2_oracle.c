@@ -14,7 +14,9 @@
  *     group / stage driver around it (cuda.c:1424-1823), for small cases;
  *   - an OpenMP batch evaluator, the timed CPU baseline;
  *   - minima_oracle.h: the periodogram of model minima of -plot mode (misc.c:65-276);
- *   - rmsd_oracle.h: the RMSD confidence intervals of chi2_gpu_rms (cuda.c:2148-2389).
+ *   - rmsd_oracle.h: the RMSD confidence intervals of chi2_gpu_rms (cuda.c:2148-2389);
+ *   - animate_oracle.h: the ANIMATE frames of compute_rgb (cuda.c:2394-2540), and
+ *     orc_model_geometry, their per-snapshot inputs.
  * Parity status: pinned bit-for-bit against a host build of the reference's own chi2one,
  * x2params and params2x compiled from its sources (oracle/build_ref.sh, tests/golden/).
  */
@@ -61,6 +63,10 @@ static void orc_ode_free(const double* y, double* f, const double* mu)
     f[2] = cos(y[1]) * (mu[0] - f[0]);
 }
 
+/* When set, chi2one also writes compute_rgb's 20 inputs of every point here (orc_model_geometry;
+ * not thread-safe, test use only). */
+static double* orc_geo_out = NULL;
+
 #define ORC_CF double
 #define ORC_SUFFIX acc
 #define ORC_FLOOR floor
@@ -102,6 +108,17 @@ void orc_model_curve(const ast_model* md, const ast_obs_set* o, const double* pa
     m2.flags &= ~AST_NUDGE;
     double dv[AST_MAX_FILTERS];
     orc_chi2one_acc(&m2, o, params, dv, vmod);
+}
+
+/* compute_rgb's inputs (b, c, E, E', S', body axes b, c, a) at every observation of o. */
+void orc_model_geometry(const ast_model* md, const ast_obs_set* o, const double* params, double* geo)
+{
+    ast_model m2 = *md;
+    m2.flags &= ~AST_NUDGE;
+    double dv[AST_MAX_FILTERS];
+    orc_geo_out = geo;
+    orc_chi2one_acc(&m2, o, params, dv, NULL);
+    orc_geo_out = NULL;
 }
 
 /* Batch of n evaluations over `threads` OpenMP threads (0 = all); the CPU baseline. */
@@ -186,3 +203,4 @@ float orc_uniform(uint64_t seed, uint64_t chain, uint32_t stage, uint32_t k)
 
 #include "minima_oracle.h"
 #include "rmsd_oracle.h"
+#include "animate_oracle.h"

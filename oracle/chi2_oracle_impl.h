@@ -185,6 +185,18 @@ ORC_CF ORC_FN(orc_chi2one)(const ast_model* md, const ast_obs_set* o, const doub
         double Sp_b = b_x * S_x1 + b_y * S_y1 + b_z * S_z1;
         double Sp_c = c_x * S_x1 + c_y * S_y1 + c_z * S_z1;
         double Sp_a = a_x * S_x1 + a_y * S_y1 + a_z * S_z1;
+        if (orc_geo_out) {
+            /* compute_rgb's inputs at this point (cuda.c:576-586). */
+            double* g = orc_geo_out + 20 * (int64_t)i;
+            g[0] = (flags & AST_BC) ? P(b) : P(b_tumb);
+            g[1] = (flags & AST_BC) ? P(c) : P(c_tumb);
+            g[2] = E_x1; g[3] = E_y1; g[4] = E_z1;
+            g[5] = Ep_b; g[6] = Ep_c; g[7] = Ep_a;
+            g[8] = Sp_b; g[9] = Sp_c; g[10] = Sp_a;
+            g[11] = b_x; g[12] = b_y; g[13] = b_z;
+            g[14] = c_x; g[15] = c_y; g[16] = c_z;
+            g[17] = a_x; g[18] = a_y; g[19] = a_z;
+        }
 
         double Vmod;
         if (flags & AST_BW_BALL) {

@@ -49,6 +49,10 @@ def load():
         lib.orc_max_threads.restype = C.c_int
         lib.orc_minima.restype = C.c_int
         lib.orc_minima.argtypes = [V, V, C.c_int, C.c_int, V, V, V, V]
+        lib.orc_render.restype = None
+        lib.orc_render.argtypes = [V, C.c_int, C.c_int, V]
+        lib.orc_model_geometry.restype = None
+        lib.orc_model_geometry.argtypes = [V, V, V, V]
         lib.orc_rmsd.restype = C.c_int
         lib.orc_rmsd.argtypes = [V, V, V, C.c_uint64, C.c_uint32, C.c_int64, C.c_int32, C.c_float, C.c_int, C.c_int,
                                  V, V, V, V, V, V, V, V]
@@ -136,6 +140,25 @@ def rmsd(model, obs, params0, seed, call, n_streams, samples, dx, reopt=1, spher
     if trace:
         out["trace_x"], out["trace_f"] = tx, tf
     return out
+
+
+def model_geometry(model, obs, params):
+    """compute_rgb's 20 inputs at every observation of obs, [n, 20]."""
+    lib = load()
+    mp, op, keep = _ptrs(model, obs)
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    geo = np.zeros((obs.n_data, 20))
+    lib.orc_model_geometry(mp, op, p.ctypes.data, geo.ctypes.data)
+    return geo
+
+
+def render(geo, size_pix):
+    """compute_rgb frames [n_frames, size_pix, size_pix, 3] (uint8) from their geometry."""
+    lib = load()
+    g = np.ascontiguousarray(geo, dtype=np.float64).reshape(-1, 20)
+    rgb = np.zeros((g.shape[0], size_pix, size_pix, 3), np.uint8)
+    lib.orc_render(g.ctypes.data, int(g.shape[0]), int(size_pix), rgb.ctypes.data)
+    return rgb
 
 
 def x2params(model, x, reopt=1):
@@ -257,6 +280,22 @@ class RefHost:
         if rc:
             raise RuntimeError("refh_params2x: tables do not match the reference build")
         return x
+
+
+def ref_render(geo):
+    """The reference's own compute_rgb on the GPU (oracle/_ref/ref_animate.cubin), 1080 x 1080."""
+    cubin = REF_DIR / "ref_animate.cubin"
+    if not cubin.exists():
+        raise FileNotFoundError(cubin)
+    lib = C.CDLL(str(HERE / "_build" / "libref_gpu_loader.so"))
+    lib.refk_render.restype = C.c_int
+    lib.refk_last_error.restype = C.c_char_p
+    g = np.ascontiguousarray(geo, dtype=np.float64).reshape(-1, 20)
+    rgb = np.zeros((g.shape[0], 1080, 1080, 3), np.uint8)
+    rc = lib.refk_render(str(cubin).encode(), C.c_void_p(g.ctypes.data), int(g.shape[0]), C.c_void_p(rgb.ctypes.data))
+    if rc:
+        raise RuntimeError(lib.refk_last_error().decode())
+    return rgb
 
 
 class RefKernel:

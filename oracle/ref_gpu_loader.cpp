@@ -111,3 +111,42 @@ done:
     }
     return rc;
 }
+
+/* The reference's compute_rgb (ref_animate.cubin, harness refa_render) for n_frames snapshots
+ * of 1080 x 1080 pixels: rgb receives n_frames * 1080 * 1080 * 3 bytes in its d_rgb layout. */
+extern "C" int refk_render(const char* cubin, const double* geo, int n_frames, unsigned char* rgb)
+{
+    int rc = 0;
+    CUdevice dev;
+    CUcontext ctx = nullptr;
+    CUmodule mod = nullptr;
+    CUfunction fr;
+    CUdeviceptr d_geo = 0, d_rgb = 0;
+    const size_t frame = (size_t)1080 * 1080 * 3;
+    CK(cuInit(0));
+    CK(cuDeviceGet(&dev, 0));
+    CK(cuDevicePrimaryCtxRetain(&ctx, dev));
+    CK(cuCtxPushCurrent(ctx));
+    CK(cuModuleLoad(&mod, cubin));
+    CK(cuModuleGetFunction(&fr, mod, "refa_render"));
+    CK(cuMemAlloc(&d_geo, sizeof(double) * 20 * (size_t)n_frames));
+    CK(cuMemAlloc(&d_rgb, frame * (size_t)n_frames));
+    CK(cuMemcpyHtoD(d_geo, geo, sizeof(double) * 20 * (size_t)n_frames));
+    for (int f = 0; f < n_frames; f++) {
+        int ff = f;
+        void* args[] = {&d_rgb, &d_geo, &ff};
+        /* 1080^2 = 2025 x 576: every thread reaches compute_rgb's __syncthreads. */
+        CK(cuLaunchKernel(fr, 2025, 1, 1, 576, 1, 1, 0, nullptr, args, nullptr));
+    }
+    CK(cuCtxSynchronize());
+    CK(cuMemcpyDtoH(rgb, d_rgb, frame * (size_t)n_frames));
+done:
+    if (d_geo) cuMemFree(d_geo);
+    if (d_rgb) cuMemFree(d_rgb);
+    if (mod) cuModuleUnload(mod);
+    if (ctx) {
+        cuCtxPopCurrent(nullptr);
+        cuDevicePrimaryCtxRelease(dev);
+    }
+    return rc;
+}
