@@ -495,6 +495,53 @@ def bench_rmsd(args, tmp, rank, world):
     print(json.dumps(line))
 
 
+def bench_animate(args, tmp, rank, world):
+    """ANIMATE frames (compute_rgb, cuda.c:2394-2540): the config-0 object's true model on the
+    ANIMATE plot grid (15 440 snapshots), 1080 x 1080 frames; frames/s of the render kernel, the
+    same through ast_render_frames with the frames copied to host memory, and the oracle."""
+    from asteroid_gb300 import api, synth
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    s = synth.generate("c0acc", tmp)
+    n_plot, S, per_step = 15440, 1080, 256
+    t, e, u = api.plot_grid(s.dir / "lc.dat", s.dir, n_plot)
+    with api.Engine(s.model, s.obs, device=local) as eng:
+        t0 = time.perf_counter()
+        geo = eng.model_geometry(s.params_true, t, e, u)
+        geo_s = time.perf_counter() - t0
+    for k in range(max(args.warmup, 3)):
+        api.render_frames(geo[:per_step], S, device=local)
+    ms, wall, frames = 0.0, 0.0, 0
+    with Clocks(local) as clk:
+        for k in range(args.steps):
+            f0 = (k * per_step) % (n_plot - per_step)
+            t0 = time.perf_counter()
+            rgb, m = api.render_frames(geo[f0:f0 + per_step], S, device=local)
+            wall += time.perf_counter() - t0
+            ms += m
+            frames += per_step
+    lit = float(np.mean(rgb[..., 0] > 0))
+    line = {"metric": "frames_per_s", "value": frames / (ms * 1e-3), "unit": "frames/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "mode": "animate",
+            "config": {"workload": f"config-0 object, {per_step} frames of {S}x{S} per step from the {n_plot}-snapshot "
+                                   "ANIMATE grid", "l2": "output frames (896 MB per step) larger than L2"},
+            "pixels_per_s": frames * S * S / (ms * 1e-3), "lit_fraction": lit, "geometry_s": geo_s,
+            "clocks": clk.summary(), "gpu_launches": args.steps,
+            "e2e": {"value": frames / wall, "unit": "frames/s", "h2d_bytes_per_step": 160 * per_step,
+                    "d2h_bytes_per_step": 3 * S * S * per_step}}
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+
+    t0 = time.perf_counter()
+    O.render(geo[:2], S)
+    cpu_s = time.perf_counter() - t0
+    line["cpu_baseline"] = {"value": 2 / cpu_s, "unit": "frames/s", "cores": 1, "kind": "port",
+                            "sample": "2 frames of 1080x1080 on one host thread"}
+    print(json.dumps(line))
+
+
 def bench_serve(args, tmp, rank, world):
     """Config 4: Poisson arrivals of config-3 objects (1024 chains x 5000 evaluations each) at 1, 4,
     16 and 64 requests/s into one server (150 GB HBM budget); p50/p99 latency from submission to
@@ -593,11 +640,12 @@ def main():
     ap.add_argument("--budget-fp64", type=int, default=0)
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-batched", action="store_true")
-    ap.add_argument("--mode", default="fit", choices=["fit", "batch", "serve", "compare", "periodogram", "rmsd"],
+    ap.add_argument("--mode", default="fit",
+                    choices=["fit", "batch", "serve", "compare", "periodogram", "rmsd", "animate"],
                     help="fit: the headline line; batch: config 3 (uneven objects, one launch); "
                          "serve: config 4 (Poisson arrivals, continuous batching); compare: full fits of "
                          "--config in both precisions at one seed; periodogram: minima() of plot mode; "
-                         "rmsd: RMSD confidence intervals")
+                         "rmsd: RMSD confidence intervals; animate: ANIMATE frames")
     ap.add_argument("--objects", type=int, default=512, help="batch mode: objects")
     ap.add_argument("--requests", type=int, default=8, help="serve mode: requests per arrival rate")
     ap.add_argument("--lanes", type=int, default=1, choices=[1, 4], help="serve mode: lanes per chain")
@@ -663,6 +711,8 @@ def main():
         return bench_periodogram(args, tmp, rank, world)
     if args.mode == "rmsd":
         return bench_rmsd(args, tmp, rank, world)
+    if args.mode == "animate":
+        return bench_animate(args, tmp, rank, world)
     s = make_workload(args, tmp)
     model, obs = s.model, s.obs
     eng = api.Engine(model, obs, device=local)
