@@ -6,9 +6,10 @@
 // the triaxial ellipsoid, Lambert-like shading between terminator, shadow and sunlit colours, a
 // red spot around the end of the b axis.  Here the recursion runs once (ast_model_geometry: one
 // thread, the fit's FP64 evaluation) and render_kernel shades every pixel of every frame from
-// that geometry: one thread per pixel, frames on the grid's y dimension, the frame's 20 doubles in
-// shared memory.  The arithmetic is the reference's, in FP64, with every rounding explicit (no
-// contracted multiply-adds) so that the CPU restatement reproduces each byte.
+// that geometry: one CTA per 32 x 8 tile of a frame, frames on the grid's y dimension, the frame's
+// 20 doubles in shared memory, each line of sight through a pixel corner evaluated once and shared
+// by the four pixels that meet there.  The arithmetic is the reference's, in FP64, with every
+// rounding explicit (no contracted multiply-adds) so that the CPU restatement reproduces each byte.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
@@ -32,12 +33,26 @@ constexpr float kSpotRad = 0.04f;  // SPOT_RAD (asteroid.h:315), a float: its sq
 #define A_(a, b) DD_ADD(a, b)
 #define S_(a, b) DD_SUB(a, b)
 
+// One CTA shades a kTileX x kTileY tile of one frame.  The four corners of a pixel are shared
+// with its neighbours, so the CTA first evaluates the (kTileX+1) x (kTileY+1) corner lines of
+// sight of its tile once each (hit, red spot, I), then every thread accumulates its pixel's four
+// corners in the reference's order (jz outer, jy inner) -- the same values, combined in the same
+// float steps, as four evaluations per pixel would give.
+constexpr int kTileX = 32, kTileY = 8;
+constexpr int kCorners = (kTileX + 1) * (kTileY + 1);
+static_assert(kTileX * kTileY == kRenderTpb, "one thread per pixel of the tile");
+
 __global__ void __launch_bounds__(kRenderTpb) render_kernel(const double* __restrict__ geo, int n_frames, int S,
                                                             uint8_t* __restrict__ rgb)
 {
     __shared__ double g[kAstGeo];
-    __shared__ double Z1x, Z1z, Y1x, Y1y, Y1z;
+    __shared__ double Z1x, Z1z, Y1x, Y1y, Y1z, A_s;
+    __shared__ double cI[kCorners];
+    __shared__ uint8_t cF[kCorners];  // bit 0: the line of sight hits the ellipsoid; bit 1: red spot
     const int f = blockIdx.y;
+    const int tiles_x = (S + kTileX - 1) / kTileX;
+    const int y0 = (blockIdx.x % tiles_x) * kTileX;  // first pixel column (iy) of the tile
+    const int z0 = (blockIdx.x / tiles_x) * kTileY;  // first pixel row (iz)
     if (threadIdx.x < kAstGeo) g[threadIdx.x] = geo[(int64_t)kAstGeo * f + threadIdx.x];
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -49,19 +64,19 @@ __global__ void __launch_bounds__(kRenderTpb) render_kernel(const double* __rest
         Y1x = M_(M_(-Ex, Ey), scale);
         Y1y = M_(A_(M_(Ex, Ex), M_(Ez, Ez)), scale);
         Y1z = M_(M_(-Ey, Ez), scale);
+        // The quadratic's A depends on the frame only (cuda.c:2454).
+        const double Epb = g[5], Epc = g[6], Epa = g[7], bb = M_(g[0], g[0]), cc = M_(g[1], g[1]);
+        A_s = A_(A_(M_(Epb, Epb) / bb, M_(Epc, Epc) / cc), M_(Epa, Epa));
     }
     __syncthreads();
-    const int id = blockIdx.x * kRenderTpb + threadIdx.x;
-    if (id >= S * S) return;
-    const int iz = id / S, iy = id % S;
-    const double b = g[0], c = g[1];
-    const double Epb = g[5], Epc = g[6], Epa = g[7], Spb = g[8], Spc = g[9], Spa = g[10];
-    const double bb = M_(b, b), cc = M_(c, c);
-    float br[3] = {0.f, 0.f, 0.f};
-    for (int jz = 0; jz < 2; jz++) {
-        const double z1 = 2.4 * (double)(iz - S / 2 + jz) / (double)S;
-        for (int jy = 0; jy < 2; jy++) {
-            const double y1 = 2.4 * (double)(iy - S / 2 + jy) / (double)S;
+    {
+        const double b = g[0], c = g[1];
+        const double Epb = g[5], Epc = g[6], Epa = g[7], Spb = g[8], Spc = g[9], Spa = g[10];
+        const double bb = M_(b, b), cc = M_(c, c), A = A_s;
+        for (int k = threadIdx.x; k < kCorners; k += kRenderTpb) {
+            const int cz = z0 + k / (kTileX + 1), cy = y0 + k % (kTileX + 1);  // corner (iz + jz, iy + jy)
+            const double z1 = 2.4 * (double)(cz - S / 2) / (double)S;
+            const double y1 = 2.4 * (double)(cy - S / 2) / (double)S;
             const double p_x = A_(M_(y1, Y1x), M_(z1, Z1x));
             const double p_y = A_(M_(y1, Y1y), M_(z1, 0.0));
             const double p_z = A_(M_(y1, Y1z), M_(z1, Z1z));
@@ -69,10 +84,11 @@ __global__ void __launch_bounds__(kRenderTpb) render_kernel(const double* __rest
             const double p_c = A_(A_(M_(g[14], p_x), M_(g[15], p_y)), M_(g[16], p_z));
             const double p_a = A_(A_(M_(g[17], p_x), M_(g[18], p_y)), M_(g[19], p_z));
             // Line of sight p + lambda E' against the ellipsoid (b, c, 1) (cuda.c:2453-2460).
-            const double A = A_(A_(M_(Epb, Epb) / bb, M_(Epc, Epc) / cc), M_(Epa, Epa));
             const double B = M_(2.0, A_(A_(M_(p_b, Epb) / bb, M_(p_c, Epc) / cc), M_(p_a, Epa)));
             const double C = S_(A_(A_(M_(p_b, p_b) / bb, M_(p_c, p_c) / cc), M_(p_a, p_a)), 1.0);
             const double D = S_(M_(B, B), M_(M_(4.0, A), C));
+            double I = 0.0;
+            uint8_t fl = 0;
             if (D >= 0.0) {
                 const double sD = sqrt(D);
                 double lambda = S_(-B, sD) / M_(2.0, A);
@@ -81,31 +97,49 @@ __global__ void __launch_bounds__(kRenderTpb) render_kernel(const double* __rest
                 const double ri_b = A_(p_b, M_(lambda, Epb));
                 const double ri_c = A_(p_c, M_(lambda, Epc));
                 const double ri_a = A_(p_a, M_(lambda, Epa));
-                const int red_spot = (A_(M_(ri_c, ri_c), M_(ri_a, ri_a)) < (double)(kSpotRad * kSpotRad) && ri_b > 0.0) ? 1 : 0;
+                const bool red_spot = A_(M_(ri_c, ri_c), M_(ri_a, ri_a)) < (double)(kSpotRad * kSpotRad) && ri_b > 0.0;
                 double ni_b = ri_b / bb, ni_c = ri_c / cc, ni_a = ri_a;
                 const double scale = 1.0 / sqrt(A_(A_(M_(ni_b, ni_b), M_(ni_c, ni_c)), M_(ni_a, ni_a)));
                 ni_b = M_(ni_b, scale);
                 ni_c = M_(ni_c, scale);
                 ni_a = M_(ni_a, scale);
-                const double I = A_(A_(M_(ni_b, Spb), M_(ni_c, Spc)), M_(ni_a, Spa));
-                // float + float + double*float, rounded back to float (cuda.c:2500-2525).
-                if (I >= 0.0) {
-                    br[0] = (float)A_((double)(br[0] + kSmaxR), M_(I, (double)(kImaxR - kSmaxR)));
-                    if (red_spot == 0) {
-                        br[1] = (float)A_((double)(br[1] + kSmaxG), M_(I, (double)(kImaxG - kSmaxG)));
-                        br[2] = (float)A_((double)(br[2] + kSmaxB), M_(I, (double)(kImaxB - kSmaxB)));
-                    }
-                } else {
-                    br[0] = (float)A_((double)(br[0] + kSmaxR), M_(I, (double)(kSmaxR - kSminR)));
-                    if (red_spot == 0) {
-                        br[1] = (float)A_((double)(br[1] + kSmaxG), M_(I, (double)(kSmaxG - kSminG)));
-                        // The reference adds to br[1] here, not br[2] (cuda.c:2523).
-                        br[2] = (float)A_((double)(br[1] + kSmaxB), M_(I, (double)(kSmaxB - kSminB)));
-                    }
+                I = A_(A_(M_(ni_b, Spb), M_(ni_c, Spc)), M_(ni_a, Spa));
+                fl = red_spot ? 3 : 1;
+            }
+            cI[k] = I;
+            cF[k] = fl;
+        }
+    }
+    __syncthreads();
+    const int ty = threadIdx.x % kTileX, tz = threadIdx.x / kTileX;
+    const int iy = y0 + ty, iz = z0 + tz;
+    if (iy >= S || iz >= S) return;
+    float br[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int jz = 0; jz < 2; jz++)
+#pragma unroll
+        for (int jy = 0; jy < 2; jy++) {
+            const int k = (tz + jz) * (kTileX + 1) + ty + jy;
+            const uint8_t fl = cF[k];
+            if (!(fl & 1)) continue;
+            const double I = cI[k];
+            const bool red_spot = (fl & 2) != 0;
+            // float + float + double*float, rounded back to float (cuda.c:2500-2525).
+            if (I >= 0.0) {
+                br[0] = (float)A_((double)(br[0] + kSmaxR), M_(I, (double)(kImaxR - kSmaxR)));
+                if (!red_spot) {
+                    br[1] = (float)A_((double)(br[1] + kSmaxG), M_(I, (double)(kImaxG - kSmaxG)));
+                    br[2] = (float)A_((double)(br[2] + kSmaxB), M_(I, (double)(kImaxB - kSmaxB)));
+                }
+            } else {
+                br[0] = (float)A_((double)(br[0] + kSmaxR), M_(I, (double)(kSmaxR - kSminR)));
+                if (!red_spot) {
+                    br[1] = (float)A_((double)(br[1] + kSmaxG), M_(I, (double)(kSmaxG - kSminG)));
+                    // The reference adds to br[1] here, not br[2] (cuda.c:2523).
+                    br[2] = (float)A_((double)(br[1] + kSmaxB), M_(I, (double)(kSmaxB - kSminB)));
                 }
             }
         }
-    }
     uint8_t* out = rgb + 3 * ((int64_t)iy + (int64_t)S * ((int64_t)iz + (int64_t)S * f));
 #pragma unroll
     for (int ic = 0; ic < 3; ic++) {
@@ -160,7 +194,7 @@ extern "C" int ast_render_frames(int32_t device, const double* geo, int32_t n_fr
     AST_CUDA(cudaStreamCreateWithFlags(&d.s, cudaStreamNonBlocking));
     AST_CUDA(cudaEventCreate(&d.e0));
     AST_CUDA(cudaEventCreate(&d.e1));
-    const unsigned blocks = (unsigned)((size_pix * size_pix + kRenderTpb - 1) / kRenderTpb);
+    const unsigned blocks = (unsigned)(((size_pix + kTileX - 1) / kTileX) * ((size_pix + kTileY - 1) / kTileY));
     double total = 0;
     for (int64_t f0 = 0; f0 < n_frames; f0 += chunk) {
         const int64_t nf = std::min<int64_t>(chunk, n_frames - f0);
