@@ -794,8 +794,10 @@ def main():
     # Phase drift of the double-float integration against FP64 over the whole light curve.
     drift = phase_drift(eng, model, obs, P[-1:] if len(P) else P, P[:7])
 
-    # End to end through the C ABI with host buffers: ast_eval_batch, copies included.
-    B = 16384
+    # End to end through the C ABI with host buffers: ast_eval_batch, copies included; four
+    # vectors per resident thread of the evaluation kernel (the fit's slot count), so the launch
+    # fills the GPU as the fit does.
+    B = 4 * (eng.fit_slots() or NCU_C2["slots"])
     Pe = workload_vectors(model, B, 21 + rank, s.params_true)
     eng.eval(Pe[:256], api.PREC_MIXED)
     t0 = time.perf_counter()
