@@ -458,6 +458,12 @@ def bench_rmsd(args, tmp, rank, world):
             "scaling": "weak", "vs_baseline": None, "data": "synthetic", "mode": "rmsd",
             "config": {"workload": "c2 object, RMSD variant, dx 1e-4, 38912 streams", "l2": "observations in shared memory"}}
     with api.Engine(m, s.obs, device=local) as eng:
+        if args.profile:   # the sampling launches only (for ncu): one model per stream, mixed
+            for k in range(args.warmup + args.steps):
+                r = eng.rmsd(s.params_true, 1e-4, n_streams=streams, samples=1, seed=1, call=k,
+                             precision=api.PREC_FP64 if args.precision == "fp64" else api.PREC_MIXED)
+            print(json.dumps({"mode": "rmsd", "models": r["n_tot"], "kernel_ms": r["kernel_ms"]}))
+            return
         for prec, name in ((api.PREC_MIXED, "mixed"), (api.PREC_FP64, "fp64")):
             r = eng.rmsd(s.params_true, 1e-4, n_streams=streams, samples=1, seed=1, precision=prec)
             per_model = r["kernel_ms"] / max(r["n_tot"], 1)
