@@ -109,7 +109,7 @@ __device__ __forceinline__ void batch_start(const BatchObj<CF>* objs, int n_objs
 
 // V.chain[s] holds the slot's global chain index; V.n_chains is the end of the chain space.
 template <class CF, int PREC, int REFILL>
-__global__ void __launch_bounds__(256, 1) batch_kernel(const BatchObj<CF>* objs, int n_objs, FitView<CF> V,
+__global__ void __launch_bounds__(KernShape<PREC>::tpb, KernShape<PREC>::min_ctas) batch_kernel(const BatchObj<CF>* objs, int n_objs, FitView<CF> V,
                                                        int64_t budget)
 {
     __shared__ float4 trig[PREC == AST_PREC_MIXED ? kTrigTable : 1];
@@ -329,7 +329,7 @@ __device__ bool coop_apply(const DevModel& M, const FitView<CF>& V, int64_t s, S
 // G = kCoopLanes lanes per slot; V.n_slots counts groups.  Dynamic shared memory: one CoopXchg
 // per group.
 template <class CF, int PREC>
-__global__ void __launch_bounds__(256, 1) coop_kernel(const BatchObj<CF>* objs, int n_objs, FitView<CF> V,
+__global__ void __launch_bounds__(KernShape<PREC>::tpb, KernShape<PREC>::min_ctas) coop_kernel(const BatchObj<CF>* objs, int n_objs, FitView<CF> V,
                                                       int64_t budget)
 {
     constexpr int G = kCoopLanes;
@@ -790,6 +790,7 @@ static int pool_geometry(ast_pool& P, int tpb, int refill)
 {
     if (P.lanes > 1) return coop_geometry<CF, PREC>(P, 128);
     if (tpb < 32 || tpb > 256 || (tpb & 31)) return ast_set_error(AST_E_INVALID, "batch: tpb must be 32..256, x32");
+    tpb = std::min(tpb, KernShape<PREC>::tpb);  // the kernel's launch bounds
     if (refill != 1 && refill != 32) return ast_set_error(AST_E_INVALID, "batch: refill must be 1 or 32");
     int occ = 0;
     AST_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel_ptr<CF, PREC>(refill), tpb, 0));
@@ -945,6 +946,7 @@ static int batch_tune_t(ast_batch* B, int64_t evals_per_slot, ast_batch_launch* 
     ast_batch_launch bt{256, 1, 0, 0.0};
     for (int r : refills)
         for (int t : tpbs) {
+            if (t > KernShape<PREC>::tpb) continue;
             double rate = 0;
             int rc = batch_probe<CF, PREC>(B, t, r, evals_per_slot, &rate);
             if (rc) return rc;

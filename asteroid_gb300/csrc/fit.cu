@@ -37,14 +37,15 @@ size_t ast_obs_smem(const ast_ctx* c);
 
 namespace ast {
 
-// MINB: CTAs of 256 threads that must fit on one SM -- 1 lets the compiler use up to 255
-// registers per thread, 2 caps it at 128 (twice the warps per SM, some spilled registers).
+// MINB: CTAs that must fit on one SM -- 1 (CTAs of up to 256) lets the compiler use up to 255
+// registers per thread, 2 caps it at 128 (twice the warps per SM, some spilled registers), 3 (CTAs
+// of up to 128) at 170: 12 warps per SM, the double-float path's best.
 //
 // Persistent slots: each slot pulls chains of the fit from an atomic pool and performs `budget`
 // evaluations (or runs until the pool is empty).  Every loop iteration is exactly one chi^2
 // evaluation per slot, so the lanes of a warp integrate in lockstep.
 template <class CF, int PREC, int MINB>
-__global__ void __launch_bounds__(256, MINB) fit_kernel(DevModel M, const void* g_obs, ObsLayout L, int use_smem,
+__global__ void __launch_bounds__(MINB == 3 ? 128 : 256, MINB) fit_kernel(DevModel M, const void* g_obs, ObsLayout L, int use_smem,
                                                         FitView<CF> V, int64_t budget)
 {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -204,7 +205,7 @@ static int fit_alloc(ast_ctx* c, int64_t slots, int64_t chains, int64_t groups, 
 template <class CF, int PREC>
 static decltype(&fit_kernel<CF, PREC, 1>) fit_kernel_ptr(int minb)
 {
-    return minb >= 2 ? fit_kernel<CF, PREC, 2> : fit_kernel<CF, PREC, 1>;
+    return minb >= 3 ? fit_kernel<CF, PREC, 3> : minb == 2 ? fit_kernel<CF, PREC, 2> : fit_kernel<CF, PREC, 1>;
 }
 
 // Launch geometry: CTA size (tpb), register budget (minb) and whether the CTA stages the
@@ -215,15 +216,23 @@ template <class CF, int PREC>
 static int fit_launch_cfg(ast_ctx* c, int tpb_req, int minb_req, int stage_req, int64_t n_chains, FitRun* r)
 {
     const size_t smem_obs = ast_obs_smem(c);
-    int minb = minb_req >= 2 ? 2 : 1;
+    // Register budget: 1 (255 registers, CTAs of up to 256), 2 (128), 3 (170, CTAs of up to 128).
+    // Unset, the kernel's own shape (KernShape): 3 for the double-float path unless the caller
+    // asks for CTAs larger than 128.
+    int minb = minb_req >= 3 ? 3 : minb_req == 2 ? 2 : minb_req == 1 ? 1 : KernShape<PREC>::min_ctas;
+    if (minb == 3 && tpb_req > 128) {
+        if (minb_req >= 3) return ast_set_error(AST_E_INVALID, "fit: min_ctas_per_sm 3 needs tpb <= 128");
+        minb = 1;
+    }
     auto kern = fit_kernel_ptr<CF, PREC>(minb);
     if (smem_obs) AST_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_obs));
     int tpb = tpb_req;
     if (tpb <= 0) {
         // Enough CTAs to cover every SM before growing the CTA (small chain counts).
         int64_t per_sm = n_chains / (c->sm_count > 0 ? c->sm_count : 1);
+        const int tpb_max = minb == 3 ? 128 : 256;
         tpb = 32;
-        while (tpb < 256 && tpb * 2 <= per_sm) tpb *= 2;
+        while (tpb < tpb_max && tpb * 2 <= per_sm) tpb *= 2;
     }
     if (tpb < 32 || tpb > 256 || (tpb & 31)) return ast_set_error(AST_E_INVALID, "fit: tpb must be 32..256, multiple of 32");
     int occ_smem = 0, occ_gmem = 0;

@@ -39,7 +39,6 @@ namespace {
 constexpr double kPi = 3.141592653589793238;  // PI (asteroid.h:16)
 constexpr double kSmall = 1e-8;                // SMALL (cuda.c:2258)
 constexpr uint32_t kRmsdDomain = 0x80000000u;  // Philox counter word 1 of RMSD draws (fit stages are below it)
-constexpr int kRmsdTpb = 256;
 
 template <class CF>
 struct RmsdView {
@@ -143,7 +142,7 @@ __device__ __forceinline__ double torque_phi(const DevModel& M, const double* p)
 }
 
 template <class CF, int PREC>
-__global__ void __launch_bounds__(kRmsdTpb, 1) rmsd_kernel(DevModel M, const void* g_obs, ObsLayout L, int use_smem,
+__global__ void __launch_bounds__(KernShape<PREC>::tpb, KernShape<PREC>::min_ctas) rmsd_kernel(DevModel M, const void* g_obs, ObsLayout L, int use_smem,
                                                            RmsdView<CF> V)
 {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -263,6 +262,7 @@ int rmsd_run(ast_ctx* c, const ast_rmsd_cfg* cfg, ast_rmsd_out* out)
     const int N = c->model.n_params;
     const size_t smem_obs = ast_obs_smem(c);
     auto kern = rmsd_kernel<CF, PREC>;
+    constexpr int kRmsdTpb = KernShape<PREC>::tpb;
     if (smem_obs) AST_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_obs));
     int occ_s = 0, occ_g = 0;
     AST_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_g, kern, kRmsdTpb, 0));
