@@ -559,7 +559,11 @@ static int pool_init(ast_pool& P, int32_t device, int32_t precision, int32_t acc
     AST_CUDA(cudaStreamCreateWithFlags(&P.stream, cudaStreamNonBlocking));
     AST_CUDA(cudaEventCreate(&P.ev0));
     AST_CUDA(cudaEventCreate(&P.ev1));
-    if (n_slots <= 0) n_slots = (int64_t)P.sm_count * 256;
+    // Default: every thread the kernel keeps resident (KernShape: 3 x 128 per SM for the
+    // double-float path, 256 for FP64).
+    if (n_slots <= 0)
+        n_slots = (int64_t)P.sm_count * (precision == AST_PREC_MIXED ? KernShape<AST_PREC_MIXED>::tpb * KernShape<AST_PREC_MIXED>::min_ctas
+                                                                     : KernShape<AST_PREC_FP64>::tpb * KernShape<AST_PREC_FP64>::min_ctas);
     P.n_slots = (n_slots + 31) / 32 * 32;
     P.S = P.n_slots;
     const int64_t S = P.S;
