@@ -43,6 +43,16 @@ struct DevModel {
     double eph_e[3][3], eph_s[3][3], eph_mjd0[3];
 };
 
+// Launch shape of the persistent evaluation kernels by precision.  The double-float path runs
+// fastest with three CTAs of 128 threads per SM (a 170-register budget, a few registers spilled:
+// 12 warps per SM instead of 8 issue-bound warps); the FP64 path is bound by its pipe and keeps
+// one CTA of 256 threads with the full register file.
+template <int PREC>
+struct KernShape {
+    static constexpr int tpb = PREC == AST_PREC_MIXED ? 128 : 256;
+    static constexpr int min_ctas = PREC == AST_PREC_MIXED ? 3 : 1;
+};
+
 // SoA observations of one object (one device buffer; also the shared-memory image).
 //   t[n]  asteroid time - hMJD0       h[n]  RK4 step of interval (i-1,i)   nst[n] its steps
 //   v[n], w[n] (float)                f[n] filter                           e{x,y,z}[n], s{x,y,z}[n]

@@ -131,16 +131,6 @@ __device__ void start_chain(const DevModel& M, const FitView<CF>& V, int64_t s, 
     for (int j = 0; j <= N; j++) IND(j) = (uint8_t)j;
 }
 
-// Launch shape of the persistent evaluation kernels by precision.  The double-float path runs
-// fastest with three CTAs of 128 threads per SM (a 170-register budget, a few registers spilled:
-// 12 warps per SM instead of 8 issue-bound warps); the FP64 path is bound by its pipe and keeps
-// one CTA of 256 threads with the full register file.
-template <int PREC>
-struct KernShape {
-    static constexpr int tpb = PREC == AST_PREC_MIXED ? 128 : 256;
-    static constexpr int min_ctas = PREC == AST_PREC_MIXED ? 3 : 1;
-};
-
 template <class CF, int PREC>
 __device__ __forceinline__ CF eval_point(const DevModel& M, const ObsView& o, const double* params, CF* dv,
                                          const float4* trig)
