@@ -114,7 +114,7 @@ int launch_prep(const DevModel& dm, char* d_block, const ObsLayout& L, int64_t n
 
 // One thread per parameter vector; the block's observations are staged into shared memory.
 template <class CF, int PREC>
-__global__ void __launch_bounds__(128, KernShape<PREC>::min_ctas) eval_kernel(DevModel M, const void* g_obs, ObsLayout L, int use_smem,
+__global__ void __launch_bounds__(128) eval_kernel(DevModel M, const void* g_obs, ObsLayout L, int use_smem,
                                                    const double* __restrict__ params, int64_t n,
                                                    double* __restrict__ chi2, double* __restrict__ dv,
                                                    unsigned long long* err)
