@@ -44,10 +44,10 @@ UNIT = "evals/s"
 # (profiles/fit_kernel_mixed_c2.md, profiles/fit_kernel_fp64_c2.md): FP32 flops of the mixed
 # path (FFMA x 2 + FADD + FMUL, the double-float formulation's own arithmetic), FP64 flops of the
 # plain path (DFMA x 2 + DADD + DMUL, including the FP64 transcendental functions), and DRAM bytes
-# of one launch over 38 912 slots (the slot state in and out; independent of the evaluations per
-# slot).  Other workloads scale the per-evaluation figures by their RK4 step count.
+# of one launch (the slot state in and out; independent of the evaluations per slot) over the
+# kernels' resident slots: 58 368 for the mixed path (three CTAs of 128 per SM), 38 912 for FP64.  Other workloads scale the per-evaluation figures by their RK4 step count.
 NCU_C2 = {"rk4_steps": 12568, "mixed_fp32_flops": 3.497e7, "fp64_flops": 7.75e6,
-          "slots": 38912, "dram_bytes_mixed": 9.97e7, "dram_bytes_fp64": 5.71e6}
+          "slots": 58368, "dram_bytes_mixed": 2.211e8, "dram_bytes_fp64": 5.71e6}
 
 
 def rk4_steps(obs, time_step):
