@@ -38,6 +38,70 @@ constexpr float kSpotRad = 0.04f;  // SPOT_RAD (asteroid.h:315), a float: its sq
 // sight of its tile once each (hit, red spot, I), then every thread accumulates its pixel's four
 // corners in the reference's order (jz outer, jy inner) -- the same values, combined in the same
 // float steps, as four evaluations per pixel would give.
+// Float pre-test of a corner line of sight.  Most lines of sight miss the ellipsoid; the
+// reference settles them with the FP64 discriminant D = B^2 - 4AC < 0.  Here D is first formed in
+// float together with a running bound on its error (each product x*y adds |x| e(y) + |y| e(x) +
+// u|xy|, each sum e(x) + e(y) + u|x+y|, u = 2^-24, the inputs carrying one rounding each).  When
+// D + 2 e(D) + 1e-12 M < 0 (M the sum of the magnitudes of D's terms, far above FP64's own
+// rounding of them), the FP64 D is negative too and the corner is background; every other corner
+// takes the reference's FP64 expressions, so the frame is the same byte for byte.
+struct ScreenF {
+    float Y1x, Y1y, Y1z, Z1x, Z1z;
+    float ax[9];  // body axes b, c, a in inertial coordinates
+    float Epb, Epc, Epa, ibb, icc, A;
+};
+
+__device__ __forceinline__ bool screen_background(const ScreenF& F, int cz, int cy, int S)
+{
+    constexpr float u = 5.9604645e-8f;  // 2^-24
+    const float fS = (float)S;
+    const float z1 = (2.4f * (float)(cz - S / 2)) / fS;
+    const float y1 = (2.4f * (float)(cy - S / 2)) / fS;
+    const float ez1 = 4.f * u * fabsf(z1), ey1 = 4.f * u * fabsf(y1);  // 2.4f, product, quotient
+    // products and sums with their error bounds
+#define PM(x, ex, y, ey, z, ez) \
+    const float z = (x) * (y); \
+    const float ez = fabsf(x) * (ey) + fabsf(y) * (ex) + u * fabsf(z);
+#define PS(x, ex, y, ey, z, ez) \
+    const float z = (x) + (y); \
+    const float ez = (ex) + (ey) + u * fabsf(z);
+    const float eY1x = u * fabsf(F.Y1x), eY1y = u * fabsf(F.Y1y), eY1z = u * fabsf(F.Y1z);
+    const float eZ1x = u * fabsf(F.Z1x), eZ1z = u * fabsf(F.Z1z);
+    PM(y1, ey1, F.Y1x, eY1x, yx, eyx) PM(z1, ez1, F.Z1x, eZ1x, zx, ezx) PS(yx, eyx, zx, ezx, px, epx)
+    PM(y1, ey1, F.Y1y, eY1y, py, epy)
+    PM(y1, ey1, F.Y1z, eY1z, yz, eyz) PM(z1, ez1, F.Z1z, eZ1z, zz, ezz) PS(yz, eyz, zz, ezz, pz, epz)
+    float pbca[3], epbca[3];
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+        const float a0 = F.ax[3 * r], a1 = F.ax[3 * r + 1], a2 = F.ax[3 * r + 2];
+        PM(a0, u * fabsf(a0), px, epx, t0, et0) PM(a1, u * fabsf(a1), py, epy, t1, et1)
+        PM(a2, u * fabsf(a2), pz, epz, t2, et2) PS(t0, et0, t1, et1, s01, es01) PS(s01, es01, t2, et2, sr, esr)
+        pbca[r] = sr;
+        epbca[r] = esr;
+    }
+    const float pb = pbca[0], pc = pbca[1], pa = pbca[2], epb = epbca[0], epc = epbca[1], epa = epbca[2];
+    const float eEpb = u * fabsf(F.Epb), eEpc = u * fabsf(F.Epc), eEpa = u * fabsf(F.Epa);
+    const float eibb = u * F.ibb, eicc = u * F.icc, eA = u * fabsf(F.A);
+    // B = 2 (pb Epb / b^2 + pc Epc / c^2 + pa Epa)
+    PM(pb, epb, F.Epb, eEpb, b1, eb1) PM(b1, eb1, F.ibb, eibb, tb, etb)
+    PM(pc, epc, F.Epc, eEpc, c1, ec1) PM(c1, ec1, F.icc, eicc, tc, etc_)
+    PM(pa, epa, F.Epa, eEpa, ta, eta) PS(tb, etb, tc, etc_, s1, es1) PS(s1, es1, ta, eta, s2, es2)
+    const float B = 2.f * s2, eB = 2.f * es2;
+    const float Babs = 2.f * (fabsf(tb) + fabsf(tc) + fabsf(ta));
+    // C = pb^2 / b^2 + pc^2 / c^2 + pa^2 - 1
+    PM(pb, epb, pb, epb, q1, eq1) PM(q1, eq1, F.ibb, eibb, qb, eqb)
+    PM(pc, epc, pc, epc, q2, eq2) PM(q2, eq2, F.icc, eicc, qc, eqc)
+    PM(pa, epa, pa, epa, qa, eqa) PS(qb, eqb, qc, eqc, r1, er1) PS(r1, er1, qa, eqa, r2, er2)
+    PS(r2, er2, -1.f, 0.f, C, eC)
+    const float Cabs = qb + qc + qa + 1.f;
+    // D = B^2 - 4 A C
+    PM(B, eB, B, eB, BB, eBB) PM(F.A, eA, C, eC, AC, eAC) PS(BB, eBB, -4.f * AC, 4.f * eAC, D, eD)
+#undef PM
+#undef PS
+    const float M = Babs * Babs + 4.f * fabsf(F.A) * Cabs;
+    return D + 2.f * eD + 1e-12f * M < 0.f;
+}
+
 constexpr int kTileX = 32, kTileY = 8;
 constexpr int kCorners = (kTileX + 1) * (kTileY + 1);
 static_assert(kTileX * kTileY == kRenderTpb, "one thread per pixel of the tile");
@@ -47,6 +111,7 @@ __global__ void __launch_bounds__(kRenderTpb) render_kernel(const double* __rest
 {
     __shared__ double g[kAstGeo];
     __shared__ double Z1x, Z1z, Y1x, Y1y, Y1z, A_s;
+    __shared__ ScreenF F;
     __shared__ double cI[kCorners];
     __shared__ uint8_t cF[kCorners];  // bit 0: the line of sight hits the ellipsoid; bit 1: red spot
     const int f = blockIdx.y;
@@ -67,6 +132,10 @@ __global__ void __launch_bounds__(kRenderTpb) render_kernel(const double* __rest
         // The quadratic's A depends on the frame only (cuda.c:2454).
         const double Epb = g[5], Epc = g[6], Epa = g[7], bb = M_(g[0], g[0]), cc = M_(g[1], g[1]);
         A_s = A_(A_(M_(Epb, Epb) / bb, M_(Epc, Epc) / cc), M_(Epa, Epa));
+        F.Y1x = (float)Y1x; F.Y1y = (float)Y1y; F.Y1z = (float)Y1z; F.Z1x = (float)Z1x; F.Z1z = (float)Z1z;
+        for (int r = 0; r < 9; r++) F.ax[r] = (float)g[11 + r];
+        F.Epb = (float)Epb; F.Epc = (float)Epc; F.Epa = (float)Epa;
+        F.ibb = (float)(1.0 / bb); F.icc = (float)(1.0 / cc); F.A = (float)A_s;
     }
     __syncthreads();
     {
@@ -75,6 +144,11 @@ __global__ void __launch_bounds__(kRenderTpb) render_kernel(const double* __rest
         const double bb = M_(b, b), cc = M_(c, c), A = A_s;
         for (int k = threadIdx.x; k < kCorners; k += kRenderTpb) {
             const int cz = z0 + k / (kTileX + 1), cy = y0 + k % (kTileX + 1);  // corner (iz + jz, iy + jy)
+            if (screen_background(F, cz, cy, S)) {
+                cI[k] = 0.0;
+                cF[k] = 0;
+                continue;
+            }
             const double z1 = 2.4 * (double)(cz - S / 2) / (double)S;
             const double y1 = 2.4 * (double)(cy - S / 2) / (double)S;
             const double p_x = A_(M_(y1, Y1x), M_(z1, Z1x));
