@@ -328,8 +328,11 @@ __device__ bool coop_apply(const DevModel& M, const FitView<CF>& V, int64_t s, S
 
 // G = kCoopLanes lanes per slot; V.n_slots counts groups.  Dynamic shared memory: one CoopXchg
 // per group.
+// Servers use cooperative chains for latency, not throughput: with the slot pool far from full a
+// chain's evaluation runs fastest with the full register file (255 registers, no spills), so this
+// kernel keeps the one-CTA-of-256 budget that the throughput kernels trade for occupancy.
 template <class CF, int PREC>
-__global__ void __launch_bounds__(KernShape<PREC>::tpb, KernShape<PREC>::min_ctas) coop_kernel(const BatchObj<CF>* objs, int n_objs, FitView<CF> V,
+__global__ void __launch_bounds__(256, 1) coop_kernel(const BatchObj<CF>* objs, int n_objs, FitView<CF> V,
                                                       int64_t budget)
 {
     constexpr int G = kCoopLanes;

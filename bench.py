@@ -654,7 +654,7 @@ def main():
                          "rmsd: RMSD confidence intervals; animate: ANIMATE frames")
     ap.add_argument("--objects", type=int, default=512, help="batch mode: objects")
     ap.add_argument("--requests", type=int, default=8, help="serve mode: requests per arrival rate")
-    ap.add_argument("--lanes", type=int, default=1, choices=[1, 4], help="serve mode: lanes per chain")
+    ap.add_argument("--lanes", type=int, default=4, choices=[1, 4], help="serve mode: lanes per chain")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--profile", action="store_true", help="only the fit launches (for ncu)")
