@@ -257,8 +257,10 @@ extern "C" int ast_render_frames(int32_t device, const double* geo, int32_t n_fr
     int rc = set_device(device);
     if (rc) return rc;
     const int64_t frame_bytes = 3ll * size_pix * size_pix;
-    // Frames per launch: at most 2 GB of pixels on the device at once (the reference uses dNPLOT).
-    const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(n_frames, (2ll << 30) / frame_bytes));
+    // Frames per launch: at most 2 GB of pixels on the device at once (the reference uses dNPLOT),
+    // and at most 65 535 (the grid's y dimension).
+    const int64_t chunk =
+        std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(n_frames, 65535), (2ll << 30) / frame_bytes));
     RenderScratch d;
     if (cudaMalloc(&d.geo, sizeof(double) * kAstGeo * chunk) != cudaSuccess ||
         cudaMalloc(&d.rgb, (size_t)(frame_bytes * chunk)) != cudaSuccess) {
