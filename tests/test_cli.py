@@ -95,6 +95,10 @@ def test_plot_mode_files(gpu, data, tmp_path):
         t, e, s = api.plot_grid(d / "lc.dat", d, 500)
         vm = eng.model_curve_at(data.params_true, t, e, s)
     assert float(line[0].split()[2].rstrip(",")) == float("%13.6e" % chi2[0])
+    # the periodogram line (asteroid.c:974-980): cl_fr then cl_H, "%f " each, of the curve + delta_V[0]
+    pg = api.minima(t, vm + dv[0, 0])
+    expect = "".join("%f " % x for x in list(pg.cl_fr) + list(pg.cl_H))
+    assert expect.strip() in [l.strip() for l in out.splitlines()]
     assert float((tmp_path / "delta_V").read_text().split()[0]) == float("%8.4f" % dv[0, 0])
     mp = (tmp_path / "model_params.dat").read_text().split()
     ids = data.model.ids
