@@ -1,6 +1,6 @@
 """Mixed-precision path (double-float RK4 on the FP32 pipe, FP32 brightness) against FP64.
 
-The bar of the benchmark spec is |dchi2|/chi2 <= 1e-6 against the FP64 result.  It is asserted
+The accuracy target of the mixed path is |dchi2|/chi2 <= 1e-6 against the FP64 result.  It is asserted
 on well-conditioned vectors (tests/test_gpu_eval.py::well_conditioned), where the FP64 result
 itself is stable to rounding; the ill-conditioned few percent, where any change of rounding
 moves chi^2, are reported but not held to it.  Under NUDGE the count of model minima is a
