@@ -106,7 +106,7 @@ constexpr int kTileX = 32, kTileY = 8;
 constexpr int kCorners = (kTileX + 1) * (kTileY + 1);
 static_assert(kTileX * kTileY == kRenderTpb, "one thread per pixel of the tile");
 
-__global__ void __launch_bounds__(kRenderTpb) render_kernel(const double* __restrict__ geo, int n_frames, int S,
+__global__ void __launch_bounds__(kRenderTpb, 3) render_kernel(const double* __restrict__ geo, int n_frames, int S,
                                                             uint8_t* __restrict__ rgb)
 {
     __shared__ double g[kAstGeo];
@@ -114,6 +114,8 @@ __global__ void __launch_bounds__(kRenderTpb) render_kernel(const double* __rest
     __shared__ ScreenF F;
     __shared__ double cI[kCorners];
     __shared__ uint8_t cF[kCorners];  // bit 0: the line of sight hits the ellipsoid; bit 1: red spot
+    __shared__ int16_t todo[kCorners];  // corners the float pre-test leaves to FP64
+    __shared__ int n_todo;
     const int f = blockIdx.y;
     const int tiles_x = (S + kTileX - 1) / kTileX;
     const int y0 = (blockIdx.x % tiles_x) * kTileX;  // first pixel column (iy) of the tile
@@ -142,13 +144,24 @@ __global__ void __launch_bounds__(kRenderTpb) render_kernel(const double* __rest
         const double b = g[0], c = g[1];
         const double Epb = g[5], Epc = g[6], Epa = g[7], Spb = g[8], Spc = g[9], Spa = g[10];
         const double bb = M_(b, b), cc = M_(c, c), A = A_s;
+        // Pass 1: the float pre-test of every corner; the undecided ones are listed.  Pass 2: the
+        // CTA's threads share the listed corners evenly, so the FP64 work (clustered on the
+        // asteroid's disc and silhouette) keeps whole warps busy instead of a few lanes.
+        if (threadIdx.x == 0) n_todo = 0;
+        __syncthreads();
         for (int k = threadIdx.x; k < kCorners; k += kRenderTpb) {
             const int cz = z0 + k / (kTileX + 1), cy = y0 + k % (kTileX + 1);  // corner (iz + jz, iy + jy)
             if (screen_background(F, cz, cy, S)) {
                 cI[k] = 0.0;
                 cF[k] = 0;
-                continue;
+            } else {
+                todo[atomicAdd(&n_todo, 1)] = (int16_t)k;
             }
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < n_todo; e += kRenderTpb) {
+            const int k = todo[e];
+            const int cz = z0 + k / (kTileX + 1), cy = y0 + k % (kTileX + 1);
             const double z1 = 2.4 * (double)(cz - S / 2) / (double)S;
             const double y1 = 2.4 * (double)(cy - S / 2) / (double)S;
             const double p_x = A_(M_(y1, Y1x), M_(z1, Z1x));
