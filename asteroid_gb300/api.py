@@ -191,7 +191,9 @@ class PeriodogramResult:
     n_minima: int
     n_clusters: int
     n_intervals: int
+    n_distinct: int
     kernel_ms: float
+    count_ms: float
 
 
 def minima(t, vm, device: int = -1) -> PeriodogramResult:
@@ -205,7 +207,8 @@ def minima(t, vm, device: int = -1) -> PeriodogramResult:
     counts = np.zeros(capi.MINIMA_BINS, np.int32)
     check(lib.ast_minima(int(device), int(t.size), dptr(t), dptr(vm), C.byref(out), iptr(counts)), "ast_minima")
     return PeriodogramResult(np.array(out.cl_fr[:]), np.array(out.cl_H[:]), counts, out.n_minima, out.n_clusters,
-                             out.n_intervals, out.kernel_ms)
+                             out.n_intervals, out.n_distinct, out.kernel_ms,
+                             out.count_ms)
 
 
 def render_frames(geo, size_pix: int = 1080, device: int = -1):

@@ -127,9 +127,11 @@ class Periodogram(C.Structure):
         ("n_minima", C.c_int32),
         ("n_clusters", C.c_int32),
         ("n_intervals", C.c_int64),
+        ("n_distinct", C.c_int64),
         ("cl_fr", C.c_double * 5),
         ("cl_H", C.c_double * 5),
         ("kernel_ms", C.c_double),
+        ("count_ms", C.c_double),
     ]
 
 

@@ -273,9 +273,11 @@ typedef struct ast_periodogram {
     int32_t n_minima;          /* minima found on the curve */
     int32_t n_clusters;        /* clusters found (<= AST_NCL_MAX) */
     int64_t n_intervals;       /* n_minima (n_minima - 1) / 2 */
+    int64_t n_distinct;        /* distinct interval values among them (each tested once, weighted) */
     double  cl_fr[AST_NCL_MAX];  /* cluster frequency (1/day), -1 where none */
     double  cl_H[AST_NCL_MAX];   /* normalised count at that frequency, 0 where none */
-    double  kernel_ms;         /* device time of the interval test */
+    double  kernel_ms;         /* device time of the interval reduction and test */
+    double  count_ms;          /* of which the test of the distinct intervals */
 } ast_periodogram;
 
 /* Curve vm at n_plot increasing times t (days) on CUDA device `device` (-1: current).  counts
