@@ -178,3 +178,28 @@ def test_plot_grid_follows_read_data(built, tmp_path, interp):
     assert np.allclose(e[1:-1], E / np.linalg.norm(E, axis=1)[:, None], rtol=0, atol=1e-10)
     assert np.allclose(s[1:-1], S / np.linalg.norm(S, axis=1)[:, None], rtol=0, atol=1e-10)
     assert np.allclose(np.linalg.norm(e, axis=1), 1.0, atol=1e-14)
+
+
+def test_cli_usage_and_argument_errors_without_a_gpu(built, tmp_path):
+    """The command line's own checks run before any device call (asteroid.c:173-445)."""
+    import subprocess
+    from asteroid_gb300 import build
+
+    cli = str(Path(build.BUILD) / "asteroid")
+    r = subprocess.run([cli], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=60)
+    assert r.returncode == 0
+    for sw in ("-best", "-i name", "-m param1", "-Nstages", "-Ppsi", "-plot", "-dx", "-i1", "-i2", "-animate"):
+        assert sw in r.stdout, sw
+    def run(*args):
+        r = subprocess.run([cli, *args], cwd=tmp_path, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True,
+                           timeout=60)
+        return r.returncode, r.stdout
+    assert run("-o", "x") == (1, "-i parameter is missing!\n")
+    rc, out = run("-i", "lc", "-plot")
+    assert rc == 1 and "require -m" in out
+    rc, out = run("-i", "lc", "-m", "1", "2")
+    assert rc == 1 and "-m can only be used together with -reopt or -plot" in out
+    rc, out = run("-i", "lc", "-bogus")
+    assert rc == 1 and "Bad arguments" in out
+    rc, out = run("-i", "lc", "-plot", "-Nplot", "1", "-m", "1")
+    assert rc == 1 and "Bad arguments" in out
