@@ -331,7 +331,7 @@ class Engine:
                                           dptr(s) if s is not None else None, dptr(out)), "ast_model_curve_at")
         return out
 
-    def rmsd(self, params0, dx: float, n_streams: int = 38912, samples: int = 1, seed: int = 1, call: int = 0,
+    def rmsd(self, params0, dx: float, n_streams: int = 116736, samples: int = 1, seed: int = 1, call: int = 0,
              precision: int = PREC_FP64, reopt: bool = True, spherical_k: bool = False, trace: bool = False) -> dict:
         """One chi2_gpu_rms call (cuda.c:2148-2389): RMSD confidence intervals of params0 over
         n_streams x samples random models (the ctx model must carry RMSD)."""
