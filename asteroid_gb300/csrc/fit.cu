@@ -217,9 +217,13 @@ static int fit_launch_cfg(ast_ctx* c, int tpb_req, int minb_req, int stage_req, 
 {
     const size_t smem_obs = ast_obs_smem(c);
     // Register budget: 1 (255 registers, CTAs of up to 256), 2 (128), 3 (170, CTAs of up to 128).
-    // Unset, the kernel's own shape (KernShape): 3 for the double-float path unless the caller
-    // asks for CTAs larger than 128.
+    // Unset, the kernel's own shape (KernShape) when the chains fill it -- 3 for the double-float
+    // path -- and the full register file when they do not: with fewer chains than three CTAs of
+    // 128 per SM hold, the extra warps would not exist and the spills would remain.
     int minb = minb_req >= 3 ? 3 : minb_req == 2 ? 2 : minb_req == 1 ? 1 : KernShape<PREC>::min_ctas;
+    if (minb_req <= 0 && minb == 3 &&
+        n_chains < (int64_t)c->sm_count * KernShape<PREC>::tpb * KernShape<PREC>::min_ctas)
+        minb = 1;
     if (minb == 3 && tpb_req > 128) {
         if (minb_req >= 3) return ast_set_error(AST_E_INVALID, "fit: min_ctas_per_sm 3 needs tpb <= 128");
         minb = 1;
