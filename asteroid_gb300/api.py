@@ -16,7 +16,8 @@ from pathlib import Path
 import numpy as np
 
 from . import capi
-from .capi import ACC, BC, BW_BALL, INTERP, NUDGE, P_PSI, PREC_FP64, PREC_MIXED, TORQUE, check, dptr, fptr, iptr
+from .capi import (ACC, BC, BW_BALL, INTERP, NUDGE, P_PSI, PREC_FP64, PREC_MIXED, PREC_MIXED_RHS32, TORQUE, check,
+                   dptr, fptr, iptr)
 
 
 def flags_from_names(names) -> int:
@@ -585,12 +586,17 @@ class Server:
         return r.value, q.value
 
     def poll(self, request):
-        """(FitResult, latency seconds) once done, else None."""
+        """(FitResult, latency seconds) once done, else None; raises AstError (AST_E_CANCELLED)
+        for a cancelled request."""
         n_chains, group, n_params, n_filters = self.items[request]
         res, out = _result(n_chains, group, n_params, n_filters)
         lat = C.c_double(0)
         rc = check(self.lib.ast_poll(self.h, int(request), C.byref(out), C.byref(lat)), "ast_poll")
         return (res, lat.value) if rc == 1 else None
+
+    def cancel(self, request) -> bool:
+        """Cancel a queued or running request (ast_cancel); False if it had already finished."""
+        return check(self.lib.ast_cancel(self.h, int(request)), "ast_cancel") == 0
 
     def request_bytes(self, request) -> int:
         return int(self.lib.ast_request_bytes(self.h, int(request)))

@@ -145,13 +145,15 @@ def build_oracle(force: bool = False) -> Path:
 def build_reference_oracle() -> None:
     """Where the reference checkout is present, build its own chi^2 code (oracle/_ref)."""
     script = ORACLE / "build_ref.sh"
-    ref = Path(os.environ.get("AST_REFERENCE_DIR", "/root/reference"))
+    ref = Path(os.environ.get("AST_REFERENCE_DIR", str(ROOT.parent / "reference")))
     if script.exists() and (ref / "cuda.c").exists():
         have = list((ORACLE / "_ref").glob("libref_*.so")) if (ORACLE / "_ref").exists() else []
         if not have:
             _run(["bash", str(script)])
         elif not (ORACLE / "_ref" / "libref_minima.so").exists():
             _run(["bash", str(script), "minima"])
+        if not (ORACLE / "_ref" / "ref_nm_ppsi_torque_acc.cubin").exists():
+            _run(["bash", str(script), "nm"])
 
 
 def build(force: bool = False) -> None:

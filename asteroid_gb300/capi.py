@@ -22,10 +22,11 @@ TORQUE, BC, BW_BALL, P_PSI, INTERP, ACC, NUDGE, RMSD = 0x01, 0x02, 0x04, 0x08, 0
 FLAG_NAMES = {"TORQUE": TORQUE, "BC": BC, "BW_BALL": BW_BALL, "P_PSI": P_PSI,
               "INTERP": INTERP, "ACC": ACC, "NUDGE": NUDGE, "RMSD": RMSD}
 PREC_FP64, PREC_MIXED = 0, 1
+PREC_MIXED_RHS32 = 2  # AST_PREC_MIXED with the ODE right-hand side in FP32
 
 STATUS = {0: "AST_OK", -1: "AST_E_INVALID", -2: "AST_E_NOMEM", -3: "AST_E_CUDA", -4: "AST_E_IO",
           -5: "AST_E_TOO_LARGE", -6: "AST_E_BUDGET", -7: "AST_E_TIMEOUT", -8: "AST_E_NOT_READY",
-          -9: "AST_E_NODEVICE"}
+          -9: "AST_E_NODEVICE", -10: "AST_E_CANCELLED"}
 
 
 class TypeIds(C.Structure):
@@ -206,6 +207,7 @@ SIGNATURES = {
                                   C.c_void_p, C.c_void_p, C.POINTER(FitCfg), C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.c_void_p]),
     "ast_fit_slots": (C.c_int64, [_P]),
+    "ast_set_stage_wait": (C.c_int, [_P, C.c_int32]),
     "ast_fit_launch": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "ast_fit_counters": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "ast_stream": (C.c_void_p, [_P]),
@@ -233,6 +235,7 @@ SIGNATURES = {
     "ast_submit": (C.c_int, [_P, C.POINTER(Model), C.POINTER(ObsSet), C.POINTER(FitCfg), C.POINTER(C.c_int64)]),
     "ast_server_step": (C.c_int, [_P, C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "ast_poll": (C.c_int, [_P, C.c_int64, C.POINTER(FitOut), C.POINTER(C.c_double)]),
+    "ast_cancel": (C.c_int, [_P, C.c_int64]),
     "ast_server_stats": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_double), C.POINTER(C.c_int64),
                                    C.POINTER(C.c_int64)]),
     "ast_request_bytes": (C.c_int64, [_P, C.c_int64]),

@@ -48,6 +48,7 @@ struct BatchObj {
     ObsLayout L;
     int64_t chain0, n_chains;
     int32_t group_size, reopt, steps_cap, fp64_result;
+    int32_t cancelled;         // ast_cancel: slots drop the object's chains (counted as finished)
     uint64_t seed;
     int64_t evals_cap;
     CF* x_start;               // [G][N] start points under reopt, else unused
@@ -161,7 +162,7 @@ __global__ void __launch_bounds__(KernShape<PREC>::tpb, KernShape<PREC>::min_cta
         if (gchain >= 0) {
             const BatchObj<CF>& B = objs[k];
             const ObsView o = B.L.view(B.obs, B.M.n_data);
-            if (slot_iterate<CF, PREC>(B.M, o, obj_view(V, B), s, R, trig, n_ev, n_fit)) {
+            if (B.cancelled || slot_iterate<CF, PREC>(B.M, o, obj_view(V, B), s, R, trig, n_ev, n_fit)) {
                 atomicAdd(B.done, 1ull);
                 n_done++;
                 gchain = -1;
@@ -377,7 +378,15 @@ __global__ void __launch_bounds__(256, 1) coop_kernel(const BatchObj<CF>* objs, 
                     batch_start<CF>(objs, n_objs, V, s, gchain, k, R);
                 }
             }
-            if (!stop) n = coop_plan<CF>(objs[k].M, obj_view(V, objs[k]), s, R, X);
+            if (!stop && objs[k].cancelled) {
+                // A cancelled request's chain is dropped (counted as finished) without a round.
+                atomicAdd(objs[k].done, 1ull);
+                n_done++;
+                gchain = -1;
+                R.chain = -1;
+            } else if (!stop) {
+                n = coop_plan<CF>(objs[k].M, obj_view(V, objs[k]), s, R, X);
+            }
         }
         stop = __shfl_sync(mask, stop, leader);
         if (stop) break;
@@ -402,7 +411,7 @@ __global__ void __launch_bounds__(256, 1) coop_kernel(const BatchObj<CF>* objs, 
             for (int m = 0; m < AST_MAX_FILTERS; m++) X.dv[r][m] = dvl[m];
         }
         __syncwarp(mask);
-        if (r == 0) {
+        if (r == 0 && gchain >= 0) {
             const BatchObj<CF>& B = objs[k];
             const FitView<CF> W = obj_view(V, B);
             bool failed = false;
@@ -477,7 +486,8 @@ struct Entry {
     size_t bytes = 0;
     int64_t off_obs = 0, off_xs = 0, off_cf = 0, off_cx = 0, off_cdv = 0, off_of = 0, off_op = 0, off_odv = 0;
     int64_t chain0 = -1;
-    int state = 0;  // 0 queued, 1 running, 2 done
+    int state = 0;  // 0 queued, 1 running, 2 done, 3 cancelled
+    bool cancel = false;  // ast_cancel on a running request: its chains are being dropped
     int done_slot = -1;
     std::vector<double> res_f, res_p, res_dv;
     double t_submit = 0, t_admit = 0, t_done = 0;
@@ -724,6 +734,7 @@ static BatchObj<CF> make_obj(const ast_pool& P, const Entry* e)
     o.reopt = e->reopt;
     o.steps_cap = e->steps_cap;
     o.fp64_result = e->fp64_result;
+    o.cancelled = e->cancel ? 1 : 0;
     o.seed = e->seed;
     o.evals_cap = e->evals_cap;
     o.x_start = (CF*)(b + e->off_xs);
@@ -1192,28 +1203,33 @@ static int server_step_t(ast_server* V, int64_t evals_per_slot, int32_t* n_runni
             AST_CUDA(cudaMemcpyAsync(P.ctr, &e0, 8, cudaMemcpyHostToDevice, P.stream));
             AST_CUDA(cudaStreamSynchronize(P.stream));
         }
-        // Retire the objects whose chains have all finished.
-        std::vector<std::pair<int, Entry*>> fin;
+        // Retire the objects whose chains have all finished (or, cancelled, have all been dropped).
+        std::vector<std::pair<int, Entry*>> fin, gone;
         for (size_t k = 0; k < P.active.size(); k++) {
             Entry* e = P.active[k];
-            if (dn[(size_t)e->done_slot] >= (unsigned long long)e->n_chains) fin.push_back({(int)k, e});
+            if (dn[(size_t)e->done_slot] >= (unsigned long long)e->n_chains) (e->cancel ? gone : fin).push_back({(int)k, e});
         }
-        if (!fin.empty()) {
+        if (!fin.empty() || !gone.empty()) {
             int n_blocks = 0;
             if ((rc = fill_gmap(P, fin, &n_blocks))) return rc;
-            batch_group_best_kernel<CF><<<(unsigned)n_blocks, 256, 0, P.stream>>>((const BatchObj<CF>*)P.d_objs,
-                                                                                 P.d_gmap, W);
-            AST_CUDA(cudaGetLastError());
-            for (auto& kv : fin) {
-                Entry* e = kv.second;
-                if ((rc = fetch_results(P, e))) return rc;
-                cudaFree(e->dev);
-                e->dev = nullptr;
-                P.hbm_used -= e->bytes;
-                P.free_done.push_back(e->done_slot);
-                e->state = 2;
-                e->t_done = now_s();
+            if (n_blocks) {
+                batch_group_best_kernel<CF><<<(unsigned)n_blocks, 256, 0, P.stream>>>((const BatchObj<CF>*)P.d_objs,
+                                                                                     P.d_gmap, W);
+                AST_CUDA(cudaGetLastError());
             }
+            for (auto& kv : fin)
+                if ((rc = fetch_results(P, kv.second))) return rc;
+            AST_CUDA(cudaStreamSynchronize(P.stream));
+            for (auto* list : {&fin, &gone})
+                for (auto& kv : *list) {
+                    Entry* e = kv.second;
+                    cudaFree(e->dev);
+                    e->dev = nullptr;
+                    P.hbm_used -= e->bytes;
+                    P.free_done.push_back(e->done_slot);
+                    e->state = e->cancel ? 3 : 2;
+                    e->t_done = now_s();
+                }
             std::vector<Entry*> keep;
             for (Entry* e : P.active)
                 if (e->state == 1) keep.push_back(e);
@@ -1242,11 +1258,33 @@ extern "C" int ast_server_step(ast_server* V, int64_t evals_per_slot, int32_t* n
     return AST_DISPATCH(V->P, server_step_t, V, evals_per_slot, n_running, n_queued);
 }
 
+extern "C" int ast_cancel(ast_server* V, int64_t request)
+{
+    if (!V || request < 0 || request >= (int64_t)V->P.all.size())
+        return ast_set_error(AST_E_INVALID, "ast_cancel: bad request");
+    Entry* e = V->P.all[(size_t)request];
+    if (e->state == 2) return 1;                         // finished: the result stays available
+    if (e->state == 3 || e->cancel) return AST_OK;       // already cancelled
+    if (e->state == 0) {                                 // queued: no device memory yet
+        auto& q = V->P.queued;
+        q.erase(std::remove(q.begin(), q.end(), e), q.end());
+        e->state = 3;
+        e->t_done = now_s();
+        return AST_OK;
+    }
+    // Running: the next ast_server_step drops its chains; once every chain is accounted for, the
+    // request retires without results and its memory returns to the budget.
+    e->cancel = true;
+    V->P.table_dirty = true;
+    return AST_OK;
+}
+
 extern "C" int ast_poll(ast_server* V, int64_t request, ast_fit_out* out, double* latency_s)
 {
     if (!V || request < 0 || request >= (int64_t)V->P.all.size())
         return ast_set_error(AST_E_INVALID, "ast_poll: bad request");
     const Entry* e = V->P.all[(size_t)request];
+    if (e->state == 3) return ast_set_error(AST_E_CANCELLED, "ast_poll: request %lld was cancelled", (long long)request);
     if (e->state != 2) return 0;
     if (out) copy_out(e, out);
     if (latency_s) *latency_s = e->t_done - e->t_submit;

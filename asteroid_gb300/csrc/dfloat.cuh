@@ -31,6 +31,7 @@
 #define DF_MUL(a, b) __fmul_rn(a, b)
 #define DF_FMA(a, b, c) __fmaf_rn(a, b, c)
 #define DF_RCP(a) __frcp_rn(a)
+#define DF_DIV(a, b) __fdiv_rn(a, b)
 #define DF_BITS(a) __float_as_int(a)
 __device__ __forceinline__ float df_rcp_approx(float a)
 {
@@ -48,12 +49,14 @@ static inline float df_h_add(float a, float b) { volatile float r = a + b; retur
 static inline float df_h_sub(float a, float b) { volatile float r = a - b; return r; }
 static inline float df_h_mul(float a, float b) { volatile float r = a * b; return r; }
 static inline float df_h_rcp(float a) { volatile float r = 1.0f / a; return r; }
+static inline float df_h_div(float a, float b) { volatile float r = a / b; return r; }
 static inline int df_h_bits(float a) { int i; memcpy(&i, &a, 4); return i; }
 #define DF_ADD(a, b) df_h_add(a, b)
 #define DF_SUB(a, b) df_h_sub(a, b)
 #define DF_MUL(a, b) df_h_mul(a, b)
 #define DF_FMA(a, b, c) fmaf(a, b, c)
 #define DF_RCP(a) df_h_rcp(a)
+#define DF_DIV(a, b) df_h_div(a, b)
 #define DF_RCP_APPROX(a) df_h_rcp(a)
 static inline double dd_h_add(double a, double b) { volatile double r = a + b; return r; }
 static inline double dd_h_sub(double a, double b) { volatile double r = a - b; return r; }

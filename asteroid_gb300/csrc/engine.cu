@@ -309,20 +309,14 @@ extern "C" void ast_destroy(ast_ctx* c)
 
 extern "C" void* ast_stream(ast_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
-// Shared memory needed to stage the object's observations, or 0 when they do not fit.
-size_t ast_obs_smem(const ast_ctx* c)
-{
-    const size_t need = (size_t)c->layout.bytes;
-    return need + 1024 <= c->smem_optin ? need : 0;
-}
-
 template <class CF, int PREC>
-static int launch_eval(ast_ctx* c, const double* d_params, int64_t n, double* d_chi2, double* d_dv, cudaStream_t s,
-                       unsigned long long* d_err)
+static int launch_eval(ast_ctx* c, const DevModel& dm, const double* d_params, int64_t n, double* d_chi2, double* d_dv,
+                       cudaStream_t s, unsigned long long* d_err)
 {
-    const size_t smem = ast_obs_smem(c);
     auto kern = eval_kernel<CF, PREC>;
-    if (smem) AST_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    size_t smem = 0;
+    int rc = obs_smem_for(kern, (size_t)c->layout.bytes, c->smem_optin, &smem);
+    if (rc) return rc;
     const int tpb = 128;
     int per_sm = 1;
     AST_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, tpb, smem));
@@ -331,7 +325,7 @@ static int launch_eval(ast_ctx* c, const double* d_params, int64_t n, double* d_
     const int64_t cap = (int64_t)c->sm_count * per_sm;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
-    kern<<<(unsigned)blocks, tpb, smem, s>>>(c->dm, c->d_obs, c->layout, smem ? 1 : 0, d_params, n, d_chi2, d_dv, d_err);
+    kern<<<(unsigned)blocks, tpb, smem, s>>>(dm, c->d_obs, c->layout, smem ? 1 : 0, d_params, n, d_chi2, d_dv, d_err);
     AST_CUDA(cudaGetLastError());
     return AST_OK;
 }
@@ -339,14 +333,16 @@ static int launch_eval(ast_ctx* c, const double* d_params, int64_t n, double* d_
 static int eval_dispatch(ast_ctx* c, int32_t precision, const double* d_params, int64_t n, double* d_chi2,
                          double* d_dv, cudaStream_t s)
 {
-    if (precision != AST_PREC_FP64 && precision != AST_PREC_MIXED)
-        return ast_set_error(AST_E_INVALID, "precision must be AST_PREC_FP64 or AST_PREC_MIXED");
+    if (precision != AST_PREC_FP64 && precision != AST_PREC_MIXED && precision != AST_PREC_MIXED_RHS32)
+        return ast_set_error(AST_E_INVALID, "precision must be AST_PREC_FP64, AST_PREC_MIXED or AST_PREC_MIXED_RHS32");
     const bool acc = (c->model.flags & AST_ACC) != 0;
+    DevModel dm = c->dm;
+    if (precision == AST_PREC_MIXED_RHS32) dm.flags |= kFlagRhs32;
     if (precision == AST_PREC_FP64)
-        return acc ? launch_eval<double, AST_PREC_FP64>(c, d_params, n, d_chi2, d_dv, s, nullptr)
-                   : launch_eval<float, AST_PREC_FP64>(c, d_params, n, d_chi2, d_dv, s, nullptr);
-    return acc ? launch_eval<double, AST_PREC_MIXED>(c, d_params, n, d_chi2, d_dv, s, nullptr)
-               : launch_eval<float, AST_PREC_MIXED>(c, d_params, n, d_chi2, d_dv, s, nullptr);
+        return acc ? launch_eval<double, AST_PREC_FP64>(c, dm, d_params, n, d_chi2, d_dv, s, nullptr)
+                   : launch_eval<float, AST_PREC_FP64>(c, dm, d_params, n, d_chi2, d_dv, s, nullptr);
+    return acc ? launch_eval<double, AST_PREC_MIXED>(c, dm, d_params, n, d_chi2, d_dv, s, nullptr)
+               : launch_eval<float, AST_PREC_MIXED>(c, dm, d_params, n, d_chi2, d_dv, s, nullptr);
 }
 
 extern "C" int ast_eval_batch_device(ast_ctx* c, int32_t precision, const double* d_params, int64_t n,
@@ -485,7 +481,7 @@ extern "C" int ast_model_geometry(ast_ctx* c, const double* params, int32_t n, c
 extern "C" int ast_model_angles(ast_ctx* c, int32_t precision, const double* params, double* angles)
 {
     if (!c || !params || !angles) return ast_set_error(AST_E_INVALID, "ast_model_angles: NULL argument");
-    if (precision != AST_PREC_FP64 && precision != AST_PREC_MIXED)
+    if (precision != AST_PREC_FP64 && precision != AST_PREC_MIXED && precision != AST_PREC_MIXED_RHS32)
         return ast_set_error(AST_E_INVALID, "ast_model_angles: bad precision");
     int rc = set_device(c->device);
     if (rc) return rc;
@@ -500,7 +496,11 @@ extern "C" int ast_model_angles(ast_ctx* c, int32_t precision, const double* par
     if (precision == AST_PREC_FP64)
         model_angles_kernel<AST_PREC_FP64><<<1, 32, 0, c->stream>>>(c->dm, c->d_obs, c->layout, dp, da);
     else
-        model_angles_kernel<AST_PREC_MIXED><<<1, 32, 0, c->stream>>>(c->dm, c->d_obs, c->layout, dp, da);
+    {
+        DevModel dm = c->dm;
+        if (precision == AST_PREC_MIXED_RHS32) dm.flags |= kFlagRhs32;
+        model_angles_kernel<AST_PREC_MIXED><<<1, 32, 0, c->stream>>>(dm, c->d_obs, c->layout, dp, da);
+    }
     AST_CUDA(cudaGetLastError());
     AST_CUDA(cudaMemcpyAsync(angles, da, sizeof(double) * 3 * c->n_data, cudaMemcpyDeviceToHost, c->stream));
     AST_CUDA(cudaStreamSynchronize(c->stream));

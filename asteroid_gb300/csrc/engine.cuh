@@ -81,9 +81,28 @@ struct ast_ctx {
     // fit
     ast::FitBuffers fb;
     ast::FitRun run;
+    int32_t stage_wait = 1 << 22;  // polls of the fit kernel's shared-memory staging wait
 };
 
 namespace ast {
+// Dynamic shared memory for staging an observation block of `bytes` in one CTA of `kern`: the
+// block's size when it fits beside the kernel's static shared memory (the double-float trig
+// table, the staging barrier) under the per-CTA opt-in limit `optin`, else 0 -- the kernel then
+// reads the block from global memory through L1.  When it is staged, the kernel's dynamic
+// shared-memory limit is raised to the block's size (needed above 48 KB; allocates nothing).
+template <class K>
+inline int obs_smem_for(K kern, size_t bytes, size_t optin, size_t* smem)
+{
+    *smem = 0;
+    if (!bytes) return AST_OK;
+    cudaFuncAttributes a;
+    AST_CUDA(cudaFuncGetAttributes(&a, kern));
+    if (bytes + a.sharedSizeBytes > optin) return AST_OK;
+    AST_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    *smem = bytes;
+    return AST_OK;
+}
+
 int build_dev_model(const ast_model* m, const ast_obs_set* obs, DevModel* dm);
 int set_device(int device);
 void obs_image(const ast_model* model, const ast_obs_set* obs, const ObsLayout& L, std::vector<unsigned char>& img);

@@ -33,8 +33,6 @@
 #include "simplex.cuh"
 #include "staging.cuh"
 
-size_t ast_obs_smem(const ast_ctx* c);
-
 namespace ast {
 
 // MINB: CTAs that must fit on one SM -- 1 (CTAs of up to 256) lets the compiler use up to 255
@@ -55,7 +53,7 @@ __global__ void __launch_bounds__(MINB == 3 ? 128 : 256, MINB) fit_kernel(DevMod
         trig_table_fill(trig);
         __syncthreads();
     }
-    const bool staged = use_smem ? bulk_stage(smem, g_obs, (uint32_t)L.bytes, &bar, &V.ctr[4]) : false;
+    const bool staged = use_smem ? bulk_stage(smem, g_obs, (uint32_t)L.bytes, &bar, &V.ctr[4], V.stage_wait) : false;
     const ObsView o = L.view(staged ? (const void*)smem : g_obs, M.n_data);
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int NF = M.n_filters;
@@ -141,6 +139,7 @@ static FitView<CF> make_view(ast_ctx* c)
     V.seed = c->run.cfg.seed;
     V.evals_cap = c->run.cfg.evals_cap;
     V.steps_cap = c->run.cfg.steps_cap > 0 ? c->run.cfg.steps_cap : 5000;
+    V.stage_wait = c->stage_wait;
     return V;
 }
 
@@ -212,28 +211,30 @@ static decltype(&fit_kernel<CF, PREC, 1>) fit_kernel_ptr(int minb)
 // observations in shared memory.  Staging is dropped when the block would lower the number of
 // CTAs an SM holds (observations are read once per observation, not per RK4 step, so global
 // reads through L1 cost little, while warps per SM decide how well latency is hidden).
+// `obs_bytes` is the observation block's size, `optin` the device's per-CTA shared-memory limit.
 template <class CF, int PREC>
-static int fit_launch_cfg(ast_ctx* c, int tpb_req, int minb_req, int stage_req, int64_t n_chains, FitRun* r)
+static int fit_launch_core(int sm_count, size_t obs_bytes, size_t optin, int tpb_req, int minb_req, int stage_req,
+                           int64_t n_chains, FitRun* r)
 {
-    const size_t smem_obs = ast_obs_smem(c);
     // Register budget: 1 (255 registers, CTAs of up to 256), 2 (128), 3 (170, CTAs of up to 128).
     // Unset, the kernel's own shape (KernShape) when the chains fill it -- 3 for the double-float
     // path -- and the full register file when they do not: with fewer chains than three CTAs of
     // 128 per SM hold, the extra warps would not exist and the spills would remain.
     int minb = minb_req >= 3 ? 3 : minb_req == 2 ? 2 : minb_req == 1 ? 1 : KernShape<PREC>::min_ctas;
     if (minb_req <= 0 && minb == 3 &&
-        n_chains < (int64_t)c->sm_count * KernShape<PREC>::tpb * KernShape<PREC>::min_ctas)
+        n_chains < (int64_t)sm_count * KernShape<PREC>::tpb * KernShape<PREC>::min_ctas)
         minb = 1;
     if (minb == 3 && tpb_req > 128) {
         if (minb_req >= 3) return ast_set_error(AST_E_INVALID, "fit: min_ctas_per_sm 3 needs tpb <= 128");
         minb = 1;
     }
     auto kern = fit_kernel_ptr<CF, PREC>(minb);
-    if (smem_obs) AST_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_obs));
+    size_t smem_obs = 0;
+    if (int rc = obs_smem_for(kern, obs_bytes, optin, &smem_obs)) return rc;
     int tpb = tpb_req;
     if (tpb <= 0) {
         // Enough CTAs to cover every SM before growing the CTA (small chain counts).
-        int64_t per_sm = n_chains / (c->sm_count > 0 ? c->sm_count : 1);
+        int64_t per_sm = n_chains / (sm_count > 0 ? sm_count : 1);
         const int tpb_max = minb == 3 ? 128 : 256;
         tpb = 32;
         while (tpb < tpb_max && tpb * 2 <= per_sm) tpb *= 2;
@@ -243,10 +244,10 @@ static int fit_launch_cfg(ast_ctx* c, int tpb_req, int minb_req, int stage_req, 
     AST_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_gmem, kern, tpb, 0));
     if (smem_obs) AST_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_smem, kern, tpb, smem_obs));
     bool stage = smem_obs != 0 && (stage_req > 0 || (stage_req == 0 && occ_smem >= occ_gmem));
-    if (stage_req > 0 && !smem_obs) stage = false;
+    if (stage && occ_smem < 1) stage = false;
     const int occ = stage ? occ_smem : occ_gmem;
     if (occ < 1) return ast_set_error(AST_E_TOO_LARGE, "fit: kernel does not fit on an SM");
-    int64_t ctas = (int64_t)c->sm_count * occ;
+    int64_t ctas = (int64_t)sm_count * occ;
     const int64_t need = (n_chains + tpb - 1) / tpb;
     if (ctas > need) ctas = need;
     if (ctas < 1) ctas = 1;
@@ -257,13 +258,20 @@ static int fit_launch_cfg(ast_ctx* c, int tpb_req, int minb_req, int stage_req, 
     return AST_OK;
 }
 
+template <class CF, int PREC>
+static int fit_launch_cfg(ast_ctx* c, int tpb_req, int minb_req, int stage_req, int64_t n_chains, FitRun* r)
+{
+    return fit_launch_core<CF, PREC>(c->sm_count, (size_t)c->layout.bytes, c->smem_optin, tpb_req, minb_req, stage_req,
+                                     n_chains, r);
+}
+
 extern "C" int ast_fit_begin(ast_ctx* c, const ast_fit_cfg* cfg)
 {
     if (!c || !cfg) return ast_set_error(AST_E_INVALID, "ast_fit_begin: NULL argument");
     if (cfg->n_chains <= 0 || cfg->group_size <= 0 || cfg->n_chains % cfg->group_size)
         return ast_set_error(AST_E_INVALID, "ast_fit_begin: n_chains must be a positive multiple of group_size");
     if (cfg->n_stages <= 0) return ast_set_error(AST_E_INVALID, "ast_fit_begin: n_stages must be >= 1");
-    if (cfg->precision != AST_PREC_FP64 && cfg->precision != AST_PREC_MIXED)
+    if (cfg->precision != AST_PREC_FP64 && cfg->precision != AST_PREC_MIXED && cfg->precision != AST_PREC_MIXED_RHS32)
         return ast_set_error(AST_E_INVALID, "ast_fit_begin: bad precision");
     if (cfg->reopt && !cfg->params0) return ast_set_error(AST_E_INVALID, "ast_fit_begin: reopt needs params0");
     if (cfg->n_stages > 1 && cfg->n_stages > 1000000) return ast_set_error(AST_E_INVALID, "ast_fit_begin: n_stages too large");
@@ -318,8 +326,10 @@ static int fit_step_t(ast_ctx* c, int64_t budget, int32_t* done, cudaStream_t s)
     FitRun& r = c->run;
     FitBuffers& b = c->fb;
     FitView<CF> V = make_view<CF>(c);
+    DevModel dm = c->dm;
+    if (r.cfg.precision == AST_PREC_MIXED_RHS32) dm.flags |= kFlagRhs32;
     AST_CUDA(cudaEventRecord(c->ev0, s));
-    fit_kernel_ptr<CF, PREC>(r.minb)<<<r.ctas, r.tpb, r.smem, s>>>(c->dm, c->d_obs, c->layout, r.smem ? 1 : 0, V, budget);
+    fit_kernel_ptr<CF, PREC>(r.minb)<<<r.ctas, r.tpb, r.smem, s>>>(dm, c->d_obs, c->layout, r.smem ? 1 : 0, V, budget);
     AST_CUDA(cudaGetLastError());
     AST_CUDA(cudaEventRecord(c->ev1, s));
     unsigned long long h[8];
@@ -328,10 +338,18 @@ static int fit_step_t(ast_ctx* c, int64_t budget, int32_t* done, cudaStream_t s)
     float ms = 0;
     AST_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
     r.kernel_ms += ms;
-    if (h[4]) return ast_set_error(AST_E_TIMEOUT, "fit: a CTA's shared-memory staging wait ran out (error word %llu)", h[4]);
+    // A staging wait that ran out is reported, not fatal: the CTAs concerned read the observations
+    // from global memory (same results) and drained their copies before exiting.  The error word
+    // is cleared for the next launch and the step completes normally (*done is valid).
+    int status = AST_OK;
+    if (h[4]) {
+        status = ast_set_error(AST_E_TIMEOUT, "fit: a CTA's shared-memory staging wait ran out (error word %llu)", h[4]);
+        AST_CUDA(cudaMemsetAsync(&b.ctr[4], 0, sizeof(unsigned long long), s));
+    }
     if (h[1] < (unsigned long long)r.cfg.n_chains) {
         *done = 0;
-        return AST_OK;
+        if (status) AST_CUDA(cudaStreamSynchronize(s));
+        return status;
     }
     // Stage finished: group argmin, hand-off or output.
     const int fp64_result = (PREC == AST_PREC_MIXED && r.cfg.fp64_result) ? 1 : 0;
@@ -343,7 +361,7 @@ static int fit_step_t(ast_ctx* c, int64_t budget, int32_t* done, cudaStream_t s)
         r.n_evals = (int64_t)h[2];
         r.n_fits = (int64_t)h[3];
         AST_CUDA(cudaStreamSynchronize(s));
-        return AST_OK;
+        return status;
     }
     r.stage++;
     r.reopt = 1;
@@ -351,7 +369,7 @@ static int fit_step_t(ast_ctx* c, int64_t budget, int32_t* done, cudaStream_t s)
     AST_CUDA(cudaMemcpyAsync(b.ctr, z, sizeof(z), cudaMemcpyHostToDevice, s));
     AST_CUDA(cudaStreamSynchronize(s));
     *done = 0;
-    return AST_OK;
+    return status;
 }
 
 extern "C" int ast_fit_step(ast_ctx* c, int64_t evals_per_slot, int32_t* done, void* stream)
@@ -382,6 +400,13 @@ extern "C" int ast_fit_counters(ast_ctx* c, int64_t* n_evals, int64_t* n_fits)
 }
 
 extern "C" int64_t ast_fit_slots(ast_ctx* c) { return c ? c->fb.slots : 0; }
+
+extern "C" int ast_set_stage_wait(ast_ctx* c, int32_t polls)
+{
+    if (!c || polls < 0) return ast_set_error(AST_E_INVALID, "ast_set_stage_wait: bad argument");
+    c->stage_wait = polls;
+    return AST_OK;
+}
 
 extern "C" int ast_fit_launch(ast_ctx* c, int32_t* tpb, int32_t* ctas, int32_t* minb, int32_t* smem)
 {
@@ -425,12 +450,18 @@ extern "C" int ast_fit(ast_ctx* c, const ast_fit_cfg* cfg, ast_fit_out* out)
     int rc = ast_fit_begin(c, cfg);
     if (rc) return rc;
     int32_t done = 0;
+    bool stage_timeout = false;
     for (int guard = 0; !done; guard++) {
-        if ((rc = ast_fit_step(c, 0, &done, nullptr))) return rc;
+        rc = ast_fit_step(c, 0, &done, nullptr);
+        if (rc == AST_E_TIMEOUT) stage_timeout = true;  // reported at the end; results unaffected
+        else if (rc) return rc;
         if (guard > 4 * cfg->n_stages + 16)
             return ast_set_error(AST_E_TIMEOUT, "ast_fit: stages did not complete");
     }
-    return ast_fit_end(c, out);
+    if ((rc = ast_fit_end(c, out))) return rc;
+    return stage_timeout ? ast_set_error(AST_E_TIMEOUT, "ast_fit: a shared-memory staging wait ran out (results "
+                                                        "read the observations from global memory)")
+                         : AST_OK;
 }
 
 // ==================================================================================== no-alloc fit
@@ -518,9 +549,10 @@ static int64_t noalloc_layout(int64_t S, int64_t C, int64_t G, int N, int NF, in
 
 template <class CF, int PREC>
 static int noalloc_run(const DevModel& dm, char* base, const int64_t* off, const ObsLayout& L, const ast_fit_cfg* cfg,
-                       int64_t S, int64_t slots, int tpb, int ctas, size_t smem, double* d_best_f, double* d_best_params,
-                       double* d_best_dv, cudaStream_t s)
+                       int64_t S, const FitRun& r, double* d_best_f, double* d_best_params, double* d_best_dv,
+                       cudaStream_t s)
 {
+    const int64_t slots = (int64_t)r.tpb * r.ctas;
     const int N = dm.n_params, NF = dm.n_filters;
     const int64_t C = cfg->n_chains, G = C / cfg->group_size;
     FitView<CF> V;
@@ -548,7 +580,8 @@ static int noalloc_run(const DevModel& dm, char* base, const int64_t* off, const
     for (int32_t stage = 0; stage < cfg->n_stages; stage++) {
         V.stage = stage;
         V.last_stage = stage == cfg->n_stages - 1;
-        fit_kernel<CF, PREC, 1><<<ctas, tpb, smem, s>>>(dm, base + off[0], L, smem ? 1 : 0, V, INT64_MAX);
+        fit_kernel_ptr<CF, PREC>(r.minb)<<<r.ctas, r.tpb, r.smem, s>>>(dm, base + off[0], L, r.smem ? 1 : 0, V,
+                                                                       INT64_MAX);
         AST_CUDA(cudaGetLastError());
         unsigned long long h[8];
         AST_CUDA(cudaMemcpyAsync(h, V.ctr, sizeof(h), cudaMemcpyDeviceToHost, s));
@@ -557,7 +590,10 @@ static int noalloc_run(const DevModel& dm, char* base, const int64_t* off, const
         if (h[1] != (unsigned long long)C)
             return ast_set_error(AST_E_TIMEOUT, "ast_fit_noalloc: stage %d finished %llu of %lld chains", stage, h[1],
                                  (long long)C);
-        group_best_kernel<CF><<<(unsigned)G, 256, 0, s>>>(dm, V, d_best_f, d_best_params, d_best_dv, nullptr, L, 0);
+        // As in ast_fit: with fp64_result a mixed search reports each group's FP64 chi^2.
+        const int fp64_result = (PREC == AST_PREC_MIXED && cfg->fp64_result) ? 1 : 0;
+        group_best_kernel<CF><<<(unsigned)G, 256, 0, s>>>(dm, V, d_best_f, d_best_params, d_best_dv, base + off[0], L,
+                                                          fp64_result);
         AST_CUDA(cudaGetLastError());
         V.reopt = 1;
         unsigned long long z[2] = {0, 0};
@@ -609,20 +645,22 @@ extern "C" int ast_fit_noalloc(const ast_model* model, const ast_obs_set* obs, c
     const bool acc = (model->flags & AST_ACC) != 0;
     const int cfb = acc ? 8 : 4;
     const ObsLayout L = ObsLayout::make(obs->n_data);
-    // Launch geometry as ast_fit_begin chooses it.
+    // Launch geometry as ast_fit_begin chooses it (CTA size, register budget, staging of the
+    // observations in shared memory, CTAs); the slots are the launch's threads.
     int sms = 0, optin = 0;
     AST_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     AST_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    const size_t smem = (size_t)L.bytes + 1024 <= (size_t)optin ? (size_t)L.bytes : 0;
-    int tpb = cfg->tpb;
-    if (tpb <= 0) {
-        const int64_t per_sm = cfg->n_chains / (sms > 0 ? sms : 1);
-        tpb = 32;
-        while (tpb < 256 && tpb * 2 <= per_sm) tpb *= 2;
-    }
-    if (tpb < 32 || tpb > 256 || (tpb & 31)) return ast_set_error(AST_E_INVALID, "ast_fit_noalloc: tpb must be 32..256");
-    const int64_t need = (cfg->n_chains + tpb - 1) / tpb;
-    const int64_t slots = need * tpb, S = (slots + 31) / 32 * 32;
+    FitRun r;
+    if (acc)
+        rc = cfg->precision == AST_PREC_FP64
+                 ? fit_launch_core<double, AST_PREC_FP64>(sms, L.bytes, optin, cfg->tpb, cfg->min_ctas_per_sm, cfg->stage_obs, cfg->n_chains, &r)
+                 : fit_launch_core<double, AST_PREC_MIXED>(sms, L.bytes, optin, cfg->tpb, cfg->min_ctas_per_sm, cfg->stage_obs, cfg->n_chains, &r);
+    else
+        rc = cfg->precision == AST_PREC_FP64
+                 ? fit_launch_core<float, AST_PREC_FP64>(sms, L.bytes, optin, cfg->tpb, cfg->min_ctas_per_sm, cfg->stage_obs, cfg->n_chains, &r)
+                 : fit_launch_core<float, AST_PREC_MIXED>(sms, L.bytes, optin, cfg->tpb, cfg->min_ctas_per_sm, cfg->stage_obs, cfg->n_chains, &r);
+    if (rc) return rc;
+    const int64_t slots = (int64_t)r.tpb * r.ctas, S = (slots + 31) / 32 * 32;
     int64_t off[20];
     const int64_t bytes = noalloc_layout(S, cfg->n_chains, cfg->n_chains / cfg->group_size, N, NF, cfb, L.bytes, off);
     if (bytes > (int64_t)AST_NOALLOC_SCRATCH_BYTES)
@@ -637,12 +675,11 @@ extern "C" int ast_fit_noalloc(const ast_model* model, const ast_obs_set* obs, c
     AST_CUDA(cudaGetLastError());
     prep_sums_kernel<<<1, 32, 0, s>>>(dm, base + off[0], L, n);
     AST_CUDA(cudaGetLastError());
-    const int ctas = (int)need;
     if (acc)
         return cfg->precision == AST_PREC_FP64
-                   ? noalloc_run<double, AST_PREC_FP64>(dm, base, off, L, cfg, S, slots, tpb, ctas, smem, d_best_f, d_best_params, d_best_dv, s)
-                   : noalloc_run<double, AST_PREC_MIXED>(dm, base, off, L, cfg, S, slots, tpb, ctas, smem, d_best_f, d_best_params, d_best_dv, s);
+                   ? noalloc_run<double, AST_PREC_FP64>(dm, base, off, L, cfg, S, r, d_best_f, d_best_params, d_best_dv, s)
+                   : noalloc_run<double, AST_PREC_MIXED>(dm, base, off, L, cfg, S, r, d_best_f, d_best_params, d_best_dv, s);
     return cfg->precision == AST_PREC_FP64
-               ? noalloc_run<float, AST_PREC_FP64>(dm, base, off, L, cfg, S, slots, tpb, ctas, smem, d_best_f, d_best_params, d_best_dv, s)
-               : noalloc_run<float, AST_PREC_MIXED>(dm, base, off, L, cfg, S, slots, tpb, ctas, smem, d_best_f, d_best_params, d_best_dv, s);
+               ? noalloc_run<float, AST_PREC_FP64>(dm, base, off, L, cfg, S, r, d_best_f, d_best_params, d_best_dv, s)
+               : noalloc_run<float, AST_PREC_MIXED>(dm, base, off, L, cfg, S, r, d_best_f, d_best_params, d_best_dv, s);
 }

@@ -137,6 +137,95 @@ AST_HD void rk4_step_df(df* y, float4 hq, float4 hw, const df* mu, const float4*
     for (int j = 0; j < NODE; j++) y[j] = yn[j];
 }
 
+// ---------------------------------------------------------------- FP32 right-hand side
+//
+// AST_PREC_MIXED_RHS32: the right-hand side of the rotation ODEs (cuda.c:26-75) in FP32 from the
+// double-float state rounded to float, the four stage derivatives K1..K4 in FP32, and the state
+// advanced in double-float, y + h/6 K1 + h/3 K2 + h/3 K3 + h/6 K4, so that the rounding of the
+// accumulated phase stays at u^2 while each step's increment carries the FP32 error of its
+// derivatives (relative ~u of h*K per step).
+
+// sin and cos of a float angle |a| <~ 4 from the shared-memory table: a = k 2pi/256 + e with
+// |e| <= pi/256, sin e = e (1 - e^2/6), cos e = 1 - e^2/2 (truncation < 2e-10).
+AST_HD void f_sincos_tab(float a, const float4* __restrict__ tab, float* s, float* c)
+{
+    const float inv_step = (float)(kTrigTable / (2.0 * 3.14159265358979323846));
+    const float magic = 12582912.0f;
+    const float kb = DF_ADD(DF_MUL(a, inv_step), magic);
+    const float k = DF_SUB(kb, magic);
+    const int idx = DF_BITS(kb) & (kTrigTable - 1);
+    const float e = DF_FMA(-k, -6.829904419802801e-10f, DF_FMA(-k, 0.02454369328916073f, a));
+    const float e2 = DF_MUL(e, e);
+    const float se = DF_MUL(e, DF_FMA(e2, -1.0f / 6.0f, 1.0f));  // sin e
+    const float hc = DF_MUL(0.5f, e2);                           // 1 - cos e
+    const float4 T = tab[idx];
+    *s = DF_FMA(T.z, se, DF_FMA(-T.x, hc, T.x));  // S cos e + C sin e
+    *c = DF_FMA(-T.x, se, DF_FMA(-T.z, hc, T.z)); // C cos e - S sin e
+}
+
+// cuda.c:46-58 in FP32.  mu as in ode_torque_df.
+AST_HD void ode_torque_f32(const float* y, float* f, const float* mu, const float4* tab)
+{
+    float s5, c5, s4, c4;
+    f_sincos_tab(y[5], tab, &s5, &c5);
+    f_sincos_tab(y[4], tab, &s4, &c4);
+    f[0] = DF_FMA(DF_MUL(mu[0], y[1]), y[2], mu[3]);
+    f[1] = DF_FMA(DF_MUL(mu[1], y[2]), y[0], mu[4]);
+    f[2] = DF_FMA(DF_MUL(mu[2], y[0]), y[1], mu[5]);
+    f[3] = DF_DIV(f_dot2(y[0], s5, y[1], c5), s4);
+    f[4] = f_dif2(y[0], c5, y[1], s5);
+    f[5] = DF_FMA(-f[3], c4, y[2]);
+}
+
+// cuda.c:69-75 in FP32: mu = (L, Ip, Im, 1 - Ip); dpsi/dt = cos(theta) L (1 - Ip + Im cos 2psi)
+// without the cancellation of L - dphi/dt.
+AST_HD void ode_free_f32(const float* y, float* f, const float* mu, const float4* tab)
+{
+    float s2, c2, s1, c1;
+    f_sincos_tab(DF_MUL(2.0f, y[2]), tab, &s2, &c2);
+    f_sincos_tab(y[1], tab, &s1, &c1);
+    f[0] = DF_MUL(mu[0], DF_FMA(-mu[2], c2, mu[1]));
+    f[1] = DF_MUL(DF_MUL(DF_MUL(mu[0], mu[2]), s1), s2);
+    f[2] = DF_MUL(DF_MUL(c1, mu[0]), DF_FMA(mu[2], c2, mu[3]));
+}
+
+// y + c*k, c a double-float, k a float (df_mad with a zero low word).
+AST_HD df df_mad_f(df y, df c, float k)
+{
+    const float p = DF_MUL(c.hi, k);
+    const float pe = DF_FMA(c.lo, k, DF_FMA(c.hi, k, -p));
+    const df s = two_sum(y.hi, p);
+    const float v = DF_ADD(DF_ADD(y.lo, pe), s.lo);
+    return fast_two_sum(s.hi, v);
+}
+
+// One RK4 step with the FP32 right-hand side.  The angle psi is brought into [-pi, pi] first so
+// that its float value (the argument of sin and cos) is accurate to u of pi; theta is bounded and
+// phi does not enter the right-hand side.
+template <int NODE>
+AST_HD void rk4_step_f32(df* y, float4 hq, float4 hw, const float* mu, const float4* tab)
+{
+    constexpr int PSI = NODE == 6 ? 5 : 2;
+    y[PSI] = df_reduce_2pi(y[PSI]);
+    float f[NODE], K[NODE];
+    df yn[NODE];
+#pragma unroll
+    for (int j = 0; j < NODE; j++) f[j] = DF_ADD(y[j].hi, y[j].lo);
+#pragma unroll 1
+    for (int st = 0; st < 4; st++) {
+        if (NODE == 6) ode_torque_f32(f, K, mu, tab); else ode_free_f32(f, K, mu, tab);
+        const float c = st < 2 ? hq.z : hq.x;                                      // h/2, h/2, h, h
+        const df wgt = (st == 1 || st == 2) ? df{hw.z, hw.w} : df{hw.x, hw.y};   // h/6, h/3, h/3, h/6
+#pragma unroll
+        for (int j = 0; j < NODE; j++) {
+            yn[j] = df_mad_f(st == 0 ? y[j] : yn[j], wgt, K[j]);
+            f[j] = DF_ADD(y[j].hi, DF_FMA(c, K[j], y[j].lo));
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < NODE; j++) y[j] = yn[j];
+}
+
 // ---------------------------------------------------------------- double-float magnitudes
 //
 // The NUDGE minimum candidates need model magnitudes far more accurate than FP32 (their
@@ -370,7 +459,9 @@ __host__ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const dou
     const double psi0 = AST_P(psi_0);
     df y[6];
     df mu[6];
+    float muf[6];  // the same constants in FP32 for the FP32 right-hand side
     const bool torque = (flags & AST_TORQUE) != 0;
+    const bool rhs32 = (flags & kFlagRhs32) != 0;
     {
         const double sp = sin(psi0);
         const double den = DD_SUB(DD_ADD(DD_MUL(DD_MUL(sp, sp), DD_SUB(Ii_inv, Is_inv)), Is_inv), 1.0);
@@ -389,13 +480,17 @@ __host__ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const dou
             y[3] = df_from_double(AST_P(phi_0));
             y[4] = df_from_double(theta);
             y[5] = df_from_double(psi0);
+            for (int k = 0; k < 6; k++) muf[k] = DF_ADD(mu[k].hi, mu[k].lo);
         } else {
             mu[0] = df_from_double(AST_P(L));
-            mu[1] = df_from_double(DD_MUL(0.5, DD_ADD(Ii_inv, Is_inv)));
+            const double Ip = DD_MUL(0.5, DD_ADD(Ii_inv, Is_inv));
+            mu[1] = df_from_double(Ip);
             mu[2] = df_from_double(DD_MUL(0.5, DD_SUB(Ii_inv, Is_inv)));
             y[0] = df_from_double(AST_P(phi_0));
             y[1] = df_from_double(theta);
             y[2] = df_from_double(psi0);
+            for (int k = 0; k < 3; k++) muf[k] = DF_ADD(mu[k].hi, mu[k].lo);
+            muf[3] = (float)DD_SUB(1.0, Ip);
         }
     }
     const bool bw = (flags & AST_BW_BALL) != 0;
@@ -416,7 +511,15 @@ __host__ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const dou
             const int N_steps = o.nst[i];
             const float4 hq = o.hq[i], hw = o.hw[i];
             // Not unrolled: one copy of the step keeps the hot loop inside the instruction cache.
-            if (torque) {
+            if (rhs32) {
+                if (torque) {
+#pragma unroll 1
+                    for (int l = 0; l < N_steps; l++) rk4_step_f32<6>(y, hq, hw, muf, tab);
+                } else {
+#pragma unroll 1
+                    for (int l = 0; l < N_steps; l++) rk4_step_f32<3>(y, hq, hw, muf, tab);
+                }
+            } else if (torque) {
 #pragma unroll 1
                 for (int l = 0; l < N_steps; l++) rk4_step_df<6>(y, hq, hw, mu, tab);
             } else {

@@ -21,6 +21,9 @@ namespace ast {
 
 constexpr double kPi = 3.141592653589793238;
 constexpr double kHuge = 1e30;
+// DevModel.flags bit outside the public AST_* variant flags: the mixed path evaluates the
+// right-hand side of the rotation ODEs in FP32 (AST_PREC_MIXED_RHS32).
+constexpr int32_t kFlagRhs32 = 1 << 20;
 
 // Tables of one variant, by value in kernel parameters (the reference's dProperty, dTypes,
 // dLimits, d_x2_params, d_chi2_params symbols, asteroid.h:460,509-513,533).

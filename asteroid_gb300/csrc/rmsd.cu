@@ -31,7 +31,6 @@
 #include "simplex.cuh"
 #include "staging.cuh"
 
-size_t ast_obs_smem(const ast_ctx* c);
 
 namespace ast {
 namespace {
@@ -260,10 +259,10 @@ template <class CF, int PREC>
 int rmsd_run(ast_ctx* c, const ast_rmsd_cfg* cfg, ast_rmsd_out* out)
 {
     const int N = c->model.n_params;
-    const size_t smem_obs = ast_obs_smem(c);
     auto kern = rmsd_kernel<CF, PREC>;
     constexpr int kRmsdTpb = KernShape<PREC>::tpb;
-    if (smem_obs) AST_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_obs));
+    size_t smem_obs = 0;
+    if (int rc = obs_smem_for(kern, (size_t)c->layout.bytes, c->smem_optin, &smem_obs)) return rc;
     int occ_s = 0, occ_g = 0;
     AST_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_g, kern, kRmsdTpb, 0));
     if (smem_obs) AST_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, kern, kRmsdTpb, smem_obs));

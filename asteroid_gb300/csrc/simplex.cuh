@@ -45,6 +45,7 @@ struct FitView {
     uint64_t seed;
     int64_t evals_cap;
     int32_t steps_cap;
+    int32_t stage_wait = 1 << 22;  // polls of the shared-memory staging wait (bulk_stage)
 };
 
 template <class CF>

@@ -32,9 +32,10 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
 }
 
 // Stage [g_obs, g_obs + L.bytes) into smem.  Must be called by every thread of the CTA.
-// `bar` is an 8-byte shared word.  Returns true when the shared copy is complete.
+// `bar` is an 8-byte shared word; each thread polls the barrier at most `wait_limit` times.
+// Returns true when the shared copy is complete.
 __device__ __forceinline__ bool bulk_stage(void* smem, const void* g_src, uint32_t bytes, uint64_t* bar,
-                                           unsigned long long* err)
+                                           unsigned long long* err, int wait_limit = kWaitLimit)
 {
     const uint32_t b = smem_u32(bar);
     if (threadIdx.x == 0) {
@@ -52,7 +53,7 @@ __device__ __forceinline__ bool bulk_stage(void* smem, const void* g_src, uint32
             : "memory");
     }
     bool ok = false;
-    for (int it = 0; it < kWaitLimit; ++it)
+    for (int it = 0; it < wait_limit; ++it)
         if (mbar_try_wait(b, 0)) { ok = true; break; }
     // Every thread must agree; one that gave up makes the whole CTA use global memory.
     ok = __syncthreads_and(ok);

@@ -40,12 +40,14 @@ METRIC = "chi2_evals_per_s"
 UNIT = "evals/s"
 
 
-# Executed work per evaluation on the config-2 workload, from ncu captures of the fit kernels
-# (profiles/fit_kernel_mixed_c2.md, profiles/fit_kernel_fp64_c2.md): FP32 flops of the mixed
-# path (FFMA x 2 + FADD + FMUL, the double-float formulation's own arithmetic), FP64 flops of the
-# plain path (DFMA x 2 + DADD + DMUL, including the FP64 transcendental functions), and DRAM bytes
-# of one launch (the slot state in and out; independent of the evaluations per slot) over the
-# kernels' resident slots: 58 368 for the mixed path (three CTAs of 128 per SM), 38 912 for FP64.  Other workloads scale the per-evaluation figures by their RK4 step count.
+# Executed work per evaluation on the config-2 workload, from ncu captures of the two fit
+# kernels (sm__sass_thread_inst_executed_op_{ffma,fadd,fmul}_pred_on.sum and the d* FP64
+# counterparts, dram__bytes_read.sum + dram__bytes_write.sum): FP32 flops of the mixed path
+# (FFMA x 2 + FADD + FMUL, the double-float formulation's own arithmetic), FP64 flops of the
+# plain path (DFMA x 2 + DADD + DMUL, including the FP64 transcendental functions), and DRAM
+# bytes of one launch (the slot state in and out; independent of the evaluations per slot) over
+# the kernels' resident slots: 58 368 for the mixed path (three CTAs of 128 per SM), 38 912 for
+# FP64.  Other workloads scale the per-evaluation figures by their RK4 step count.
 NCU_C2 = {"rk4_steps": 12568, "mixed_fp32_flops": 3.497e7, "fp64_flops": 7.75e6,
           "slots": 58368, "dram_bytes_mixed": 2.211e8, "dram_bytes_fp64": 5.71e6}
 
@@ -255,6 +257,27 @@ def run_batch_steps(s, precision, n_chains, group, evals_cap, budget, warmup, st
     return (e1 - e0) / (t[0] * 1e-3)
 
 
+def measure_fits(device, chains=4096, evals=2000, seed=777):
+    """Completed fits per second, measured: config 0 (300 points, LS + TORQUE + P_PSI, FP64
+    simplex) run to completion -- `chains` random-start chains of `evals` chi^2 evaluations each
+    (ast_fit, one stage, groups of 256) -- in each precision; device time of the simplex launches.
+    A fit is one chain, as in the reference (one chain per thread)."""
+    from asteroid_gb300 import api, synth
+
+    with tempfile.TemporaryDirectory() as d:
+        s = synth.generate("c0acc", d)
+        out = {"workload": f"c0: {s.obs.n_data} points, {api.flag_names(s.model.flags)}, {chains} chains x "
+                           f"{evals} evals, one stage, run to completion"}
+        with api.Engine(s.model, s.obs, device=device) as eng:
+            eng.fit(n_chains=256, group_size=256, seed=seed, evals_cap=20)  # warm-up
+            for prec, name in ((api.PREC_MIXED, "mixed"), (api.PREC_FP64, "fp64")):
+                r = eng.fit(n_chains=chains, group_size=256, seed=seed, evals_cap=evals, precision=prec)
+                sec = r.kernel_ms * 1e-3
+                out[name] = {"fits_per_s": r.n_fits / sec, "evals_per_s": r.n_evals / sec, "seconds": sec,
+                             "n_fits": r.n_fits, "n_evals": r.n_evals, "best_chi2": float(r.best_f.min())}
+    return out
+
+
 def wrap(a):
     return (a + np.pi) % (2 * np.pi) - np.pi
 
@@ -448,6 +471,60 @@ def bench_periodogram(args, tmp, rank, world):
     line["plot_c2"] = {"model_curve_ms": 1e3 * (t1 - t0), "minima_ms": 1e3 * (t2 - t1), "n_minima": rp.n_minima,
                        "cl_fr": list(rp.cl_fr)}
     print(json.dumps(line))
+
+
+def bench_precisions(args, tmp, rank, world):
+    """The three evaluation precisions on one configuration: chi^2 evaluations/s of the fit kernel
+    (bounded resumable launches, the headline's timing) and the relative chi^2 error against FP64
+    on the workload's vectors whose FP64 chi^2 is stable to a one-ulp move of the parameters,
+    plus the Euler-angle drift of each mixed form over the light curve."""
+    import torch
+
+    from asteroid_gb300 import api
+
+    s = make_workload(args, tmp)
+    model, obs = s.model, s.obs
+    reopt = bool(model.flags & api.NUDGE)
+    p0 = s.params_true if reopt else None
+    out = {"mode": "precisions", "config": args.config, "n_data": obs.n_data, "chains": args.chains,
+           "model": api.flag_names(model.flags)}
+    with api.Engine(model, obs) as eng:
+        stream = torch.cuda.ExternalStream(eng.stream)
+
+        def timed(fn):
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            r = fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            return a.elapsed_time(b), r
+
+        P = np.vstack([workload_vectors(model, 2047, 11, s.params_true), s.params_true[None, :]])
+        c64, _ = eng.eval(P, api.PREC_FP64)
+        Q = P * (1 + np.random.default_rng(0).choice([-1.0, 1.0], size=P.shape) * 2.3e-16)
+        q64, _ = eng.eval(Q, api.PREC_FP64)
+        with np.errstate(invalid="ignore", divide="ignore"):
+            cond = np.abs(q64 - c64) / np.abs(c64)
+        good = np.isfinite(c64) & (c64 < 1e29) & (cond <= 1e-10)
+        for prec, name in ((api.PREC_FP64, "fp64"), (api.PREC_MIXED, "mixed"), (api.PREC_MIXED_RHS32, "mixed_rhs32")):
+            ev, ms, _, _, b = run_fit_steps(eng, prec, args.chains, 256, args.evals_cap, 0, 2, 3, 1234, timed, reopt, p0)
+            row = {"evals_per_s": ev / (ms * 1e-3), "budget": b}
+            if prec != api.PREC_FP64:
+                c, _ = eng.eval(P, prec)
+                ok = good & (c < 1e29)
+                rel = np.abs(c[ok] - c64[ok]) / np.abs(c64[ok])
+                drift = 0.0
+                for p in P[-1:]:
+                    a64, a = eng.model_angles(p, api.PREC_FP64), eng.model_angles(p, prec)
+                    drift = max(drift, float(np.abs(wrap(a - a64)).max()))
+                row.update({"vectors": int(ok.sum()), "median_rel": float(np.median(rel)),
+                            "p99_rel": float(np.quantile(rel, 0.99)), "max_rel": float(rel.max()),
+                            "frac_le_1e-6": float(np.mean(rel <= 1e-6)),
+                            "true_model_rel": float(abs(c[-1] - c64[-1]) / abs(c64[-1])),
+                            "true_model_angle_drift_rad": drift})
+            out[name] = row
+    print(json.dumps(out))
 
 
 def bench_rmsd(args, tmp, rank, world):
@@ -654,8 +731,9 @@ def main():
     ap.add_argument("--budget-fp64", type=int, default=0)
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-batched", action="store_true")
+    ap.add_argument("--skip-fits", action="store_true", help="skip the full-length config-0 fits")
     ap.add_argument("--mode", default="fit",
-                    choices=["fit", "batch", "serve", "compare", "periodogram", "rmsd", "animate"],
+                    choices=["fit", "batch", "serve", "compare", "periodogram", "rmsd", "animate", "precisions"],
                     help="fit: the headline line; batch: config 3 (uneven objects, one launch); "
                          "serve: config 4 (Poisson arrivals, continuous batching); compare: full fits of "
                          "--config in both precisions at one seed; periodogram: minima() of plot mode; "
@@ -727,6 +805,8 @@ def main():
         return bench_rmsd(args, tmp, rank, world)
     if args.mode == "animate":
         return bench_animate(args, tmp, rank, world)
+    if args.mode == "precisions":
+        return bench_precisions(args, tmp, rank, world)
     s = make_workload(args, tmp)
     model, obs = s.model, s.obs
     eng = api.Engine(model, obs, device=local)
@@ -774,6 +854,7 @@ def main():
         ev_m, ms_m, fits_m, launches_m, b_mixed = run_fit_steps(
             eng, api.PREC_MIXED, args.chains, 256, args.evals_cap, args.budget_mixed, args.warmup, args.steps, seed,
             timed, reopt, p0)
+    slots_m = eng.fit_slots() or NCU_C2["slots"]  # the mixed launch's resident slots
     ms_m = max_over_ranks(dist, ms_m)
     ev_m_all = sum_over_ranks(dist, ev_m)
     value = ev_m_all / (ms_m * 1e-3)
@@ -811,7 +892,7 @@ def main():
     # End to end through the C ABI with host buffers: ast_eval_batch, copies included; four
     # vectors per resident thread of the evaluation kernel (the fit's slot count), so the launch
     # fills the GPU as the fit does.
-    B = 4 * (eng.fit_slots() or NCU_C2["slots"])
+    B = 4 * slots_m
     Pe = workload_vectors(model, B, 21 + rank, s.params_true)
     eng.eval(Pe[:256], api.PREC_MIXED)
     t0 = time.perf_counter()
@@ -824,9 +905,14 @@ def main():
     peak32 = api.probe_peak("fp32", local)
     peak64 = api.probe_peak("fp64", local)
     scale = n_rk4 / NCU_C2["rk4_steps"]
-    slots = eng.fit_slots() or NCU_C2["slots"]
-    achieved = NCU_C2["mixed_fp32_flops"] * scale * value / 1e12 / max(world, 1)
-    achieved64 = NCU_C2["fp64_flops"] * scale * fp64 / 1e12 / max(world, 1) if fp64 else None
+    # Algorithmic work: the reference source's flop count per evaluation (flops) times the
+    # evaluations per second; executed work: the FP32 (mixed) or FP64 flops ncu counts per
+    # evaluation of these kernels.
+    achieved = flops * value / 1e12 / max(world, 1)
+    executed = NCU_C2["mixed_fp32_flops"] * scale * value / 1e12 / max(world, 1)
+    achieved64 = flops * fp64 / 1e12 / max(world, 1) if fp64 else None
+    executed64 = NCU_C2["fp64_flops"] * scale * fp64 / 1e12 / max(world, 1) if fp64 else None
+    fits = measure_fits(local) if (rank == 0 and world == 1 and not args.skip_fits) else None
     cpu = cpu_baseline(model, obs, args.cpu_seconds, s.params_true) if (rank == 0 and world == 1) else None
     clocks = clk.summary()
 
@@ -843,7 +929,8 @@ def main():
                                    f"timed slice of {b_mixed} evals/slot/step", "chains_per_gpu": args.chains,
                        "n_data": obs.n_data, "rk4_steps_per_eval": n_rk4, "parallelism": f"replicas x{world}",
                        "l2": "flushed before every timed region (256 MB write); simplex state ~100 MB, obs in smem"},
-            "fits_per_s": value / args.evals_cap,
+            "fits_per_s": fits["mixed"]["fits_per_s"] if fits else None,
+            "fits": fits,
             "fp64": {"value": fp64, "unit": UNIT, "speedup_mixed_over_fp64": (value / fp64) if fp64 else None},
             "batched": None if batched is None else {
                 "value": batched, "unit": UNIT, "speedup_over_fp64": (batched / fp64) if fp64 else None,
@@ -857,19 +944,26 @@ def main():
                                  "the parameters (cond <= 1e-10)"},
             "roofline": {"bound": "fp32 pipe (CUDA cores)", "achieved": achieved, "peak": peak32 / 1e3,
                          "unit": "TFLOP/s", "frac": achieved / (peak32 / 1e3),
-                         "traffic": NCU_C2["dram_bytes_mixed"] * slots / NCU_C2["slots"],
+                         "traffic": NCU_C2["dram_bytes_mixed"] * slots_m / NCU_C2["slots"],
                          "kernel": "fit_kernel<double, MIXED>",
-                         "per_eval": {"fp32_flops": NCU_C2["mixed_fp32_flops"] * scale,
-                                      "source": "ncu FFMA x 2 + FADD + FMUL per evaluation "
-                                                "(profiles/fit_kernel_mixed_c2.md)"},
-                         "reference_flops_per_eval": flops, "reference_gflops": flops * value / 1e9,
-                         "transcendentals_per_eval": trans,
+                         "per_eval": {"flops": flops, "transcendentals": trans,
+                                      "source": "the reference's chi2one counted from its source: 152 per RK4 "
+                                                "step, 156 per observation, 6 per filter, 50 per evaluation "
+                                                "(add/mul/div/sqrt 1, fma 2); transcendental calls not counted"},
+                         "executed": {"achieved": executed, "frac": executed / (peak32 / 1e3),
+                                      "fp32_flops_per_eval": NCU_C2["mixed_fp32_flops"] * scale,
+                                      "source": "ncu FFMA x 2 + FADD + FMUL per evaluation of this kernel "
+                                                "(the double-float formulation's own arithmetic)"},
                          "peak_source": "measured in this run by ast_probe_peak (FP32 FMA loop over every SM); "
                                         "MEASURED_PEAKS.json holds HBM and bf16 only",
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch of the "
+                                           "config-2 capture, scaled by this launch's resident slots",
                          "fp64_path": {"kernel": "fit_kernel<double, FP64>", "bound": "fp64 pipe",
                                        "achieved": achieved64, "peak": peak64 / 1e3, "unit": "TFLOP/s",
                                        "frac": (achieved64 / (peak64 / 1e3)) if achieved64 else None,
-                                       "per_eval_fp64_flops": NCU_C2["fp64_flops"] * scale}},
+                                       "executed": executed64,
+                                       "executed_frac": (executed64 / (peak64 / 1e3)) if executed64 else None,
+                                       "per_eval_fp64_flops_executed": NCU_C2["fp64_flops"] * scale}},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": B * model.n_params * 8,
                     "d2h_bytes_per_step": B * (1 + obs.n_filters) * 8, "path": "ast_eval_batch, mixed, host buffers"},

@@ -54,6 +54,7 @@ extern "C" {
 #define AST_E_TIMEOUT     -7   /* a device wait gave up after its iteration limit */
 #define AST_E_NOT_READY   -8   /* result not available yet */
 #define AST_E_NODEVICE    -9   /* no CUDA device */
+#define AST_E_CANCELLED  -10   /* the request was cancelled (ast_cancel) */
 
 /* ---------------------------------------------------------------- model variants
  * The reference selects these with compile-time macros (makefile:1-36); here they are
@@ -193,7 +194,10 @@ int ast_format_result(char* buf, int64_t cap, double chi2, const double* dv, int
 typedef struct ast_ctx ast_ctx;
 
 #define AST_PREC_FP64   0   /* plain path: the reference's double arithmetic */
-#define AST_PREC_MIXED  1   /* FP32 right-hand side and brightness, double-FP32 state */
+#define AST_PREC_MIXED  1   /* double-FP32 state and right-hand side, FP32 brightness */
+#define AST_PREC_MIXED_RHS32 2 /* AST_PREC_MIXED with the ODE right-hand side in FP32 (the state
+                                  still double-FP32): faster, but outside 1e-6 relative chi^2 on
+                                  about 5-10% of vectors; single-object evaluation and fits only */
 
 /* gpu_prepare.c:2-56 + asteroid.c:603-606: pack one object's observations into SoA device
  * buffers (16-byte aligned segments staged into shared memory by bulk copies), hoist the
@@ -361,7 +365,10 @@ int ast_rmsd(ast_ctx* ctx, const ast_rmsd_cfg* cfg, ast_rmsd_out* out);
 
 /* The same pass split into resumable launches: chain state stays resident on the device
  * between ast_fit_step calls.  Each step lets every chain slot perform at most
- * evals_per_slot evaluations; *done becomes 1 when all stages of all chains finished. */
+ * evals_per_slot evaluations; *done becomes 1 when all stages of all chains finished.
+ * AST_E_TIMEOUT from ast_fit_step (or ast_fit) means a CTA's shared-memory staging wait ran
+ * out and it read the observations from global memory instead: the step is complete, *done is
+ * valid and the results are unaffected; the fit may continue. */
 int ast_fit_begin(ast_ctx* ctx, const ast_fit_cfg* cfg);
 int ast_fit_step(ast_ctx* ctx, int64_t evals_per_slot, int32_t* done, void* stream);
 int ast_fit_end(ast_ctx* ctx, ast_fit_out* out);
@@ -387,6 +394,13 @@ int ast_fit_noalloc(const ast_model* model, const ast_obs_set* obs, const double
                     const float* d_w, const int32_t* d_filter, const double* d_e_unit, const double* d_s_unit,
                     const ast_fit_cfg* cfg, double* d_best_f, double* d_best_params, double* d_best_dv,
                     void* stream);
+
+/* How many times each thread of the fit kernel polls the barrier of the shared-memory staging
+ * copy before it gives up (default 4194304; no reference counterpart).  A CTA whose wait runs out
+ * reads the observations from global memory instead (the results do not change), waits for its
+ * copy before it exits, and the step returns AST_E_TIMEOUT.  0 takes that path at once: the
+ * device-side failure path can be exercised without a fault. */
+int ast_set_stage_wait(ast_ctx* ctx, int32_t polls);
 
 /* Number of chain slots (persistent threads) the fit kernel of this context runs. */
 int64_t ast_fit_slots(ast_ctx* ctx);
@@ -469,8 +483,15 @@ int ast_submit(ast_server* server, const ast_model* model, const ast_obs_set* ob
                int64_t* request);
 int ast_server_step(ast_server* server, int64_t evals_per_slot, int32_t* n_running, int32_t* n_queued);
 /* 1 and the result (and the seconds from ast_submit to retirement) once the request is done,
- * 0 while it is queued or running, < 0 on error. */
+ * 0 while it is queued or running, AST_E_CANCELLED after ast_cancel, < 0 on other errors. */
 int ast_poll(ast_server* server, int64_t request, ast_fit_out* out, double* latency_s);
+/* Cancel a request (no reference counterpart: the reference runs one fit per process).  A queued
+ * request leaves the queue at once.  A running one is dropped by the next ast_server_step: its
+ * slots abandon its chains and take other work, and once every chain is accounted for, the
+ * request retires without results and its device memory returns to the HBM budget; the other
+ * requests' results do not change.  Returns 0, or 1 when the request had already finished (its
+ * result stays available). */
+int ast_cancel(ast_server* server, int64_t request);
 int ast_server_stats(ast_server* server, int64_t* n_evals, double* kernel_ms, int64_t* hbm_used,
                      int64_t* hbm_budget);
 /* Device bytes the request holds while admitted (what admission counts against the budget). */

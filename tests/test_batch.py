@@ -158,3 +158,36 @@ def test_cooperative_chains_equal_single_fits(gpu, synth_objects, precision):
         same(got[k], ref)
         total += ref.n_evals
     assert evals == total  # only the evaluations the one-lane chains make are counted
+
+
+@pytest.mark.parametrize("lanes", [1, 4])
+def test_server_cancel_queued_and_running(gpu, synth_objects, lanes):
+    """ast_cancel on a queued request removes it before admission; on a running request the next
+    step drops its chains, its memory returns to the HBM budget, and ast_poll reports
+    AST_E_CANCELLED.  The other requests' results are those of their single fits, bit for bit."""
+    objs = [synth_objects(n) for n in ("c3_0", "c3_1", "c3_2", "c3_3")]
+    cfg = dict(CFG, evals_cap=200)
+    with api.Server(precision=api.PREC_MIXED, acc=True, n_slots=152 * 64, lanes=lanes) as srv:
+        ids = [srv.submit(s.model, s.obs, **dict(cfg, seed=80 + k)) for k, s in enumerate(objs)]
+        assert srv.cancel(ids[3])                      # still queued: never admitted
+        srv.step(4)                                    # admits 0..2, which start to run
+        used_before = srv.stats()["hbm_used"]
+        assert used_before >= sum(srv.request_bytes(i) for i in ids[:3])
+        assert srv.cancel(ids[1])                      # running
+        srv.step(4)
+        assert srv.stats()["hbm_used"] <= used_before - srv.request_bytes(ids[1])
+        for i in (ids[1], ids[3]):
+            with pytest.raises(api.capi.AstError) as ei:
+                srv.poll(i)
+            assert ei.value.code == -10
+        while any(srv.poll(i) is None for i in (ids[0], ids[2])):
+            srv.step(16)
+        got = {i: srv.poll(i)[0] for i in (ids[0], ids[2])}
+        assert not srv.cancel(ids[0])                  # finished: the result stays
+        assert srv.stats()["hbm_used"] == 0
+    for k in (0, 2):
+        s = objs[k]
+        with api.Engine(s.model, s.obs) as eng:
+            ref = eng.fit(n_chains=cfg["n_chains"], group_size=cfg["group_size"], seed=80 + k,
+                          evals_cap=cfg["evals_cap"], precision=api.PREC_MIXED)
+        same(got[ids[k]], ref)
