@@ -121,6 +121,32 @@ def build_engine(force: bool = False, ptxas_verbose: bool = False) -> Path:
     return lib
 
 
+PARITY = BUILD / "parity"
+
+
+def build_parity_engine(force: bool = False) -> Path:
+    """The engine with engine.cu -- the evaluation kernels behind ast_eval_batch -- compiled
+    without fused multiply-adds (nvcc -fmad=false), linked with the other objects of the main
+    build into _build/parity/libasteroid_gb300.so.  Test infrastructure for the FP64 parity
+    check against the reference kernel compiled the same way (oracle/build_ref.sh nofma): both
+    sides then round every product and sum separately, so only the order of operations and
+    CUDA's libm are left to differ.  Loaded in a child process through AST_ENGINE_LIB."""
+    build_engine()
+    PARITY.mkdir(exist_ok=True)
+    nvcc = _nvcc()
+    src = PKG / "csrc" / "engine.cu"
+    obj = PARITY / "engine.o"
+    if force or _stale(obj, [src] + _headers()):
+        _run([nvcc, *GENCODE, "-lineinfo", "-O3", "-std=c++17", "-fmad=false", "-Xcompiler",
+              "-fPIC,-O2,-ffp-contract=off", f"-I{INCLUDE}", f"-I{PKG / 'host'}", "-c", str(src), "-o", str(obj)])
+    objs = [obj] + [BUILD / (Path(s).stem + ".o") for s in CU_SOURCES if Path(s).stem != "engine"]
+    objs += [BUILD / (Path(s).stem + ".o") for s in C_SOURCES]
+    lib = PARITY / "libasteroid_gb300.so"
+    if force or _stale(lib, objs):
+        _run([nvcc, *GENCODE, "-shared", "-o", str(lib), *map(str, objs), "-lcudart", *_zlib()[1]])
+    return lib
+
+
 def build_oracle(force: bool = False) -> Path:
     """Compile the CPU oracle (test infrastructure) with OpenMP and without fused multiply-adds."""
     ORACLE_BUILD.mkdir(exist_ok=True)
@@ -154,6 +180,8 @@ def build_reference_oracle() -> None:
             _run(["bash", str(script), "minima"])
         if not (ORACLE / "_ref" / "ref_nm_ppsi_torque_acc.cubin").exists():
             _run(["bash", str(script), "nm"])
+        if not (ORACLE / "_ref" / "ref_ppsi_torque_acc_nofma.cubin").exists():
+            _run(["bash", str(script), "nofma"])
 
 
 def build(force: bool = False) -> None:

@@ -246,7 +246,10 @@ _LIB = None
 
 
 def lib_path() -> Path:
-    return Path(__file__).resolve().parent / "_build" / "libasteroid_gb300.so"
+    """The in-tree engine library; AST_ENGINE_LIB names another build of it (the parity test's
+    build without fused multiply-adds)."""
+    env = os.environ.get("AST_ENGINE_LIB")
+    return Path(env) if env else Path(__file__).resolve().parent / "_build" / "libasteroid_gb300.so"
 
 
 def load() -> C.CDLL:

@@ -473,6 +473,86 @@ def bench_periodogram(args, tmp, rank, world):
     print(json.dumps(line))
 
 
+def reference_workload(name):
+    """The config's object from tests/golden/workload_<name>.npz (tests/golden/make_workload.py)
+    as (model, obs, true parameters), built without the engine library: the ast_model bytes and
+    the converted observation arrays."""
+    from asteroid_gb300 import api, capi
+
+    z = np.load(ROOT / "tests" / "golden" / f"workload_{name}.npz")
+    model = capi.Model.from_buffer_copy(z["model"].tobytes())
+    obs = api.Obs(z["mjd"], z["v"], z["w"], z["filt"], z["e_unit"], z["s_unit"], z["eph_e"], z["eph_s"], z["eph_mjd0"],
+                  z["t_min"], z["v_min"], float(z["hmjd0"][0]))
+    return model, obs, z["params_true"]
+
+
+def reference_vectors(O, model, n, seed, params_true, radius=0.02):
+    """workload_vectors through the oracle's own x2params / params2x (the reference arm loads no
+    engine code): the prior with resolved rotation, or for NUDGE a jitter around the truth."""
+    from asteroid_gb300 import capi
+
+    rng = np.random.default_rng(seed)
+    out = []
+    if model.flags & capi.NUDGE:
+        x0 = O.params2x(model, params_true)
+        while len(out) < n:
+            p = O.x2params(model, x0 + rng.uniform(-radius, radius, model.n_params), reopt=1)
+            if p is not None:
+                out.append(p)
+    else:
+        iL = model.types[model.ids.L]
+        while len(out) < n:
+            p = O.x2params(model, rng.uniform(0, 1, model.n_params), reopt=0)
+            if p is not None and p[iL] * model.time_step <= 0.5:
+                out.append(p)
+    return np.array(out)
+
+
+def bench_reference(args):
+    """The CPU implementation of the path on the host cores: the oracle port of the reference's
+    chi2one (OpenMP, all threads) on the config's object, no engine code loaded."""
+    from asteroid_gb300 import build
+
+    build.build_oracle()
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+
+    model, obs, p_true = reference_workload(args.config)
+    threads = O.max_threads()
+    P = reference_vectors(O, model, threads, 5, p_true)
+    for _ in range(1 + args.warmup):
+        O.chi2_batch(model, obs, P, threads=threads)
+    t0 = time.perf_counter()
+    O.chi2_batch(model, obs, P, threads=threads)
+    n = max(threads, int(args.cpu_seconds * 2 / 3 / max(time.perf_counter() - t0, 1e-6) * threads))
+    P = reference_vectors(O, model, n, 6, p_true)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        O.chi2_batch(model, obs, P, threads=threads)
+        times.append(time.perf_counter() - t0)
+    v = n * args.steps / sum(times)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (tests/golden/workload_" + args.config + ".npz)",
+            "config": {"workload": f"{args.config}: chi2one on {n} parameter vectors per step"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{n} vectors per step; the reference's host build is x86-only, so the "
+                                       f"oracle port of its chi2one runs on this host"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "engine_library_loaded": engine_library_loaded()}
+    print(json.dumps(line))
+
+
+def engine_library_loaded() -> bool:
+    """Whether this process has mapped libasteroid_gb300.so (Linux /proc/self/maps)."""
+    try:
+        return "libasteroid_gb300" in Path("/proc/self/maps").read_text()
+    except OSError:
+        return False
+
+
 def bench_precisions(args, tmp, rank, world):
     """The three evaluation precisions on one configuration: chi^2 evaluations/s of the fit kernel
     (bounded resumable launches, the headline's timing) and the relative chi^2 error against FP64
@@ -752,40 +832,7 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        from asteroid_gb300 import api, build, synth
-
-        build.build_engine()
-        sys.path.insert(0, str(ROOT / "oracle"))
-        import oracle as O
-
-        s = synth.generate(args.config, tmp, vmod_fn=lambda m, o, p: O.model_curve(m, o, p))
-        build.build_oracle()
-        threads = O.max_threads()
-        P = workload_vectors(s.model, threads, 5, s.params_true)
-        O.chi2_batch(s.model, s.obs, P, threads=threads)
-        for _ in range(args.warmup):
-            O.chi2_batch(s.model, s.obs, P, threads=threads)
-        t0 = time.perf_counter()
-        O.chi2_batch(s.model, s.obs, P, threads=threads)
-        per_step = 10.0
-        n = max(threads, int(per_step / max(time.perf_counter() - t0, 1e-6) * threads))
-        P = workload_vectors(s.model, n, 6, s.params_true)
-        times = []
-        for _ in range(args.steps):
-            t0 = time.perf_counter()
-            O.chi2_batch(s.model, s.obs, P, threads=threads)
-            times.append(time.perf_counter() - t0)
-        v = n * args.steps / sum(times)
-        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic", "config": {"workload": f"{args.config}: chi2one on {n} parameter vectors per step"},
-                "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                                 "sample": f"{n} vectors per step; the reference's host build is x86-only, so the "
-                                           f"oracle port of its chi2one runs on this host"},
-                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
-        return
+        return bench_reference(args)
 
     import torch
 

@@ -12,6 +12,8 @@
 #                        oracle/ref_harness_minima.cu; pins the periodogram oracle.
 #   ref_animate.cubin    device build (sm_100) of cuda.c with -DANIMATE plus
 #                        oracle/ref_harness_animate.cu: the reference's compute_rgb on the GPU.
+#   ref_<variant>_nofma.cubin  the same device build with nvcc -fmad=false (no multiply-add
+#                        contraction), for the parity check against the engine built the same way.
 #   ref_nm_<variant>.cubin  device build (sm_100) of cuda.c whose setup_kernel + chi2_gpu
 #                        (cuda.c:2039,1326) run on the GPU through refn_fit in
 #                        oracle/ref_gpu_loader.cpp; three instrumentation hooks are inserted in
@@ -106,7 +108,15 @@ if [[ "${1:-all}" == "all" || "${1:-all}" == "cubin" || "${1:-all}" == "nm" ]]; 
         pids+=($!)
     done
 fi
-[[ "${1:-all}" == "minima" || "${1:-all}" == "animate" || "${1:-all}" == "nm" ]] && VARIANTS=()
+if [[ "${1:-all}" == "all" || "${1:-all}" == "cubin" || "${1:-all}" == "nofma" ]]; then
+    for v in "${VARIANTS[@]}"; do
+        read -r name ts macros <<<"$v"
+        ( stream_source "$ts" 0 | nvcc -x cu -cubin -arch=sm_100 -O3 -fmad=false -DMAIN $macros -I"$REF" -w \
+              -o "$OUT/ref_${name}_nofma.cubin" - ) &
+        pids+=($!)
+    done
+fi
+[[ "${1:-all}" == "minima" || "${1:-all}" == "animate" || "${1:-all}" == "nm" || "${1:-all}" == "nofma" ]] && VARIANTS=()
 for v in "${VARIANTS[@]}"; do
     read -r name ts macros <<<"$v"
     if [[ "${1:-all}" == "all" || "${1:-all}" == "host" ]]; then
