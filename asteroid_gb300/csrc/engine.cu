@@ -121,8 +121,8 @@ __global__ void __launch_bounds__(128) eval_kernel(DevModel M, const void* g_obs
 {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t bar;
-    __shared__ float4 trig[PREC == AST_PREC_MIXED ? kTrigTable : 1];
-    if (PREC == AST_PREC_MIXED) {
+    __shared__ float4 trig[PREC != AST_PREC_FP64 ? kTrigTable : 1];
+    if (PREC != AST_PREC_FP64) {
         trig_table_fill(trig);
         __syncthreads();
     }
@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(128) eval_kernel(DevModel M, const void* g_obs
         if (PREC == AST_PREC_FP64)
             r = chi2_fp64<CF>(M, o, p, d);
         else
-            r = chi2_mixed<CF>(M, o, p, d, trig);
+            r = chi2_mixed<CF, PREC == AST_PREC_MIXED_RHS32>(M, o, p, d, trig);
         chi2[k] = (double)r;
         if (dv)
             for (int m = 0; m < M.n_filters; m++) dv[k * M.n_filters + m] = (double)d[m];
@@ -176,7 +176,7 @@ __global__ void model_angles_kernel(DevModel M, const void* g_obs, ObsLayout L, 
     DevModel M2 = M;
     M2.flags &= ~AST_NUDGE;
     if (PREC == AST_PREC_FP64) chi2_fp64<double>(M2, o, p, d, nullptr, ang);
-    else chi2_mixed<double>(M2, o, p, d, trig, ang);
+    else chi2_mixed<double, PREC == AST_PREC_MIXED_RHS32>(M2, o, p, d, trig, ang);
 }
 
 // FMA throughput probe (roofline denominators for CUDA-core bound kernels).
@@ -336,11 +336,13 @@ static int eval_dispatch(ast_ctx* c, int32_t precision, const double* d_params, 
     if (precision != AST_PREC_FP64 && precision != AST_PREC_MIXED && precision != AST_PREC_MIXED_RHS32)
         return ast_set_error(AST_E_INVALID, "precision must be AST_PREC_FP64, AST_PREC_MIXED or AST_PREC_MIXED_RHS32");
     const bool acc = (c->model.flags & AST_ACC) != 0;
-    DevModel dm = c->dm;
-    if (precision == AST_PREC_MIXED_RHS32) dm.flags |= kFlagRhs32;
+    const DevModel& dm = c->dm;
     if (precision == AST_PREC_FP64)
         return acc ? launch_eval<double, AST_PREC_FP64>(c, dm, d_params, n, d_chi2, d_dv, s, nullptr)
                    : launch_eval<float, AST_PREC_FP64>(c, dm, d_params, n, d_chi2, d_dv, s, nullptr);
+    if (precision == AST_PREC_MIXED_RHS32)
+        return acc ? launch_eval<double, AST_PREC_MIXED_RHS32>(c, dm, d_params, n, d_chi2, d_dv, s, nullptr)
+                   : launch_eval<float, AST_PREC_MIXED_RHS32>(c, dm, d_params, n, d_chi2, d_dv, s, nullptr);
     return acc ? launch_eval<double, AST_PREC_MIXED>(c, dm, d_params, n, d_chi2, d_dv, s, nullptr)
                : launch_eval<float, AST_PREC_MIXED>(c, dm, d_params, n, d_chi2, d_dv, s, nullptr);
 }
@@ -495,12 +497,10 @@ extern "C" int ast_model_angles(ast_ctx* c, int32_t precision, const double* par
     AST_CUDA(cudaMemcpyAsync(dp, params, sizeof(double) * c->model.n_params, cudaMemcpyHostToDevice, c->stream));
     if (precision == AST_PREC_FP64)
         model_angles_kernel<AST_PREC_FP64><<<1, 32, 0, c->stream>>>(c->dm, c->d_obs, c->layout, dp, da);
+    else if (precision == AST_PREC_MIXED_RHS32)
+        model_angles_kernel<AST_PREC_MIXED_RHS32><<<1, 32, 0, c->stream>>>(c->dm, c->d_obs, c->layout, dp, da);
     else
-    {
-        DevModel dm = c->dm;
-        if (precision == AST_PREC_MIXED_RHS32) dm.flags |= kFlagRhs32;
-        model_angles_kernel<AST_PREC_MIXED><<<1, 32, 0, c->stream>>>(dm, c->d_obs, c->layout, dp, da);
-    }
+        model_angles_kernel<AST_PREC_MIXED><<<1, 32, 0, c->stream>>>(c->dm, c->d_obs, c->layout, dp, da);
     AST_CUDA(cudaGetLastError());
     AST_CUDA(cudaMemcpyAsync(angles, da, sizeof(double) * 3 * c->n_data, cudaMemcpyDeviceToHost, c->stream));
     AST_CUDA(cudaStreamSynchronize(c->stream));

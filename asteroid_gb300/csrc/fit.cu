@@ -48,8 +48,8 @@ __global__ void __launch_bounds__(MINB == 3 ? 128 : 256, MINB) fit_kernel(DevMod
 {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t bar;
-    __shared__ float4 trig[PREC == AST_PREC_MIXED ? kTrigTable : 1];
-    if (PREC == AST_PREC_MIXED) {
+    __shared__ float4 trig[PREC != AST_PREC_FP64 ? kTrigTable : 1];
+    if (PREC != AST_PREC_FP64) {
         trig_table_fill(trig);
         __syncthreads();
     }
@@ -286,12 +286,15 @@ extern "C" int ast_fit_begin(ast_ctx* c, const ast_fit_cfg* cfg)
     const bool acc = (c->model.flags & AST_ACC) != 0;
     const int cfb = acc ? 8 : 4;
     const int mb = cfg->min_ctas_per_sm, so = cfg->stage_obs;
+    const int32_t pr = cfg->precision;
     if (acc)
-        rc = cfg->precision == AST_PREC_FP64 ? fit_launch_cfg<double, AST_PREC_FP64>(c, cfg->tpb, mb, so, cfg->n_chains, &r)
-                                             : fit_launch_cfg<double, AST_PREC_MIXED>(c, cfg->tpb, mb, so, cfg->n_chains, &r);
+        rc = pr == AST_PREC_FP64        ? fit_launch_cfg<double, AST_PREC_FP64>(c, cfg->tpb, mb, so, cfg->n_chains, &r)
+             : pr == AST_PREC_MIXED_RHS32 ? fit_launch_cfg<double, AST_PREC_MIXED_RHS32>(c, cfg->tpb, mb, so, cfg->n_chains, &r)
+                                        : fit_launch_cfg<double, AST_PREC_MIXED>(c, cfg->tpb, mb, so, cfg->n_chains, &r);
     else
-        rc = cfg->precision == AST_PREC_FP64 ? fit_launch_cfg<float, AST_PREC_FP64>(c, cfg->tpb, mb, so, cfg->n_chains, &r)
-                                             : fit_launch_cfg<float, AST_PREC_MIXED>(c, cfg->tpb, mb, so, cfg->n_chains, &r);
+        rc = pr == AST_PREC_FP64        ? fit_launch_cfg<float, AST_PREC_FP64>(c, cfg->tpb, mb, so, cfg->n_chains, &r)
+             : pr == AST_PREC_MIXED_RHS32 ? fit_launch_cfg<float, AST_PREC_MIXED_RHS32>(c, cfg->tpb, mb, so, cfg->n_chains, &r)
+                                        : fit_launch_cfg<float, AST_PREC_MIXED>(c, cfg->tpb, mb, so, cfg->n_chains, &r);
     if (rc) return rc;
     const int64_t slots = (int64_t)r.tpb * r.ctas;
     const int64_t groups = cfg->n_chains / cfg->group_size;
@@ -326,10 +329,8 @@ static int fit_step_t(ast_ctx* c, int64_t budget, int32_t* done, cudaStream_t s)
     FitRun& r = c->run;
     FitBuffers& b = c->fb;
     FitView<CF> V = make_view<CF>(c);
-    DevModel dm = c->dm;
-    if (r.cfg.precision == AST_PREC_MIXED_RHS32) dm.flags |= kFlagRhs32;
     AST_CUDA(cudaEventRecord(c->ev0, s));
-    fit_kernel_ptr<CF, PREC>(r.minb)<<<r.ctas, r.tpb, r.smem, s>>>(dm, c->d_obs, c->layout, r.smem ? 1 : 0, V, budget);
+    fit_kernel_ptr<CF, PREC>(r.minb)<<<r.ctas, r.tpb, r.smem, s>>>(c->dm, c->d_obs, c->layout, r.smem ? 1 : 0, V, budget);
     AST_CUDA(cudaGetLastError());
     AST_CUDA(cudaEventRecord(c->ev1, s));
     unsigned long long h[8];
@@ -352,7 +353,7 @@ static int fit_step_t(ast_ctx* c, int64_t budget, int32_t* done, cudaStream_t s)
         return status;
     }
     // Stage finished: group argmin, hand-off or output.
-    const int fp64_result = (PREC == AST_PREC_MIXED && r.cfg.fp64_result) ? 1 : 0;
+    const int fp64_result = (PREC != AST_PREC_FP64 && r.cfg.fp64_result) ? 1 : 0;
     group_best_kernel<CF><<<(unsigned)b.groups, 256, 0, s>>>(c->dm, V, b.out_f, b.out_p, b.out_dv, c->d_obs,
                                                                c->layout, fp64_result);
     AST_CUDA(cudaGetLastError());
@@ -384,6 +385,9 @@ extern "C" int ast_fit_step(ast_ctx* c, int64_t evals_per_slot, int32_t* done, v
     if (c->run.cfg.precision == AST_PREC_FP64)
         return acc ? fit_step_t<double, AST_PREC_FP64>(c, evals_per_slot, done, s)
                    : fit_step_t<float, AST_PREC_FP64>(c, evals_per_slot, done, s);
+    if (c->run.cfg.precision == AST_PREC_MIXED_RHS32)
+        return acc ? fit_step_t<double, AST_PREC_MIXED_RHS32>(c, evals_per_slot, done, s)
+                   : fit_step_t<float, AST_PREC_MIXED_RHS32>(c, evals_per_slot, done, s);
     return acc ? fit_step_t<double, AST_PREC_MIXED>(c, evals_per_slot, done, s)
                : fit_step_t<float, AST_PREC_MIXED>(c, evals_per_slot, done, s);
 }

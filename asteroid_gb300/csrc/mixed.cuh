@@ -423,14 +423,207 @@ static __host__ __device__ __noinline__ bool nudge_flush(const DevModel& M, cons
     return true;
 }
 
+// Per-evaluation constants of the FP32 magnitude: the spin-axis frame (cuda.c:195-217) and the
+// photometric shape (cuda.c:568-574) or the BW_BALL parameters.
+struct MixedFrame {
+    float M_x, M_y, M_z, XM_x, XM_z, YM_x, YM_y, YM_z;
+    float ib, ic, bc;
+    float kappa, cos_phR, sin_phR, cos_thR, sin_thR;
+};
+constexpr int kMixedFrameFloats = 16;
+
+// The integrated state of one evaluation of the mixed path: y and the ODE constants mu as
+// double-floats (and in FP32 for the FP32 right-hand side), the magnitude frame.
+struct MixedState {
+    df y[6];
+    df mu[6];
+    float muf[6];
+    bool torque, bw;
+    MixedFrame F;
+};
+
+// Per-evaluation set-up in FP64 (cuda.c:195-252): initial Euler angles and angular velocity, the
+// ODE constants, the magnitude frame.  Every rounding explicit (DD_*, DF_*, f_*, d_*), with float
+// and double operands as in the reference's expressions: the same bits in every kernel.
+AST_HD void mixed_setup(const DevModel& M, const double* params, MixedState& S)
+{
+    const int flags = M.flags;
+    const ast_type_ids& T = M.t;
+#define AST_P(tt) params[M.idx[T.tt]]
+    const double th_M = AST_P(theta_M), ph_M = AST_P(phi_M);
+    const double M_xd = DD_MUL(sin(th_M), cos(ph_M)), M_yd = DD_MUL(sin(th_M), sin(ph_M)), M_zd = cos(th_M);
+    const double XMd = sqrt(d_dot2(M_zd, M_zd, M_xd, M_xd));
+    MixedFrame& F = S.F;
+    F.M_x = (float)M_xd;
+    F.M_y = (float)M_yd;
+    F.M_z = (float)M_zd;
+    F.XM_x = (float)(M_zd / XMd);
+    F.XM_z = (float)(-M_xd / XMd);
+    F.YM_x = DF_MUL(F.M_y, F.XM_z);
+    F.YM_y = f_dif2(F.M_z, F.XM_x, F.M_x, F.XM_z);
+    F.YM_z = -DF_MUL(F.M_y, F.XM_x);
+    const double bt = AST_P(b_tumb), ct = AST_P(c_tumb);
+    const double bt2 = DD_MUL(bt, bt), ct2 = DD_MUL(ct, ct);
+    const double Is = DD_ADD(1.0, bt2) / DD_ADD(bt2, ct2);
+    const double Ii = DD_ADD(1.0, ct2) / DD_ADD(bt2, ct2);
+    const double Is_inv = 1.0 / Is, Ii_inv = 1.0 / Ii;
+    const double psi0 = AST_P(psi_0);
+    S.torque = (flags & AST_TORQUE) != 0;
+    {
+        const double sp = sin(psi0);
+        const double den = DD_SUB(DD_ADD(DD_MUL(DD_MUL(sp, sp), DD_SUB(Ii_inv, Is_inv)), Is_inv), 1.0);
+        const double theta = asin(sqrt(DD_SUB(AST_P(Es), 1.0) / den));
+        if (S.torque) {
+            S.mu[0] = df_from_double(DD_MUL(DD_SUB(Is, 1.0), Ii_inv));
+            S.mu[1] = df_from_double(DD_MUL(DD_SUB(1.0, Ii), Is_inv));
+            S.mu[2] = df_from_double(DD_SUB(Ii, Is));
+            S.mu[3] = df_from_double(AST_P(Ti));
+            S.mu[4] = df_from_double(AST_P(Ts));
+            S.mu[5] = df_from_double(AST_P(Tl));
+            const double L = AST_P(L);
+            S.y[0] = df_from_double(DD_MUL(DD_MUL(DD_MUL(L, Ii_inv), sin(theta)), sp));
+            S.y[1] = df_from_double(DD_MUL(DD_MUL(DD_MUL(L, Is_inv), sin(theta)), cos(psi0)));
+            S.y[2] = df_from_double(DD_MUL(L, cos(theta)));
+            S.y[3] = df_from_double(AST_P(phi_0));
+            S.y[4] = df_from_double(theta);
+            S.y[5] = df_from_double(psi0);
+            for (int k = 0; k < 6; k++) S.muf[k] = DF_ADD(S.mu[k].hi, S.mu[k].lo);
+        } else {
+            S.mu[0] = df_from_double(AST_P(L));
+            const double Ip = DD_MUL(0.5, DD_ADD(Ii_inv, Is_inv));
+            S.mu[1] = df_from_double(Ip);
+            S.mu[2] = df_from_double(DD_MUL(0.5, DD_SUB(Ii_inv, Is_inv)));
+            S.y[0] = df_from_double(AST_P(phi_0));
+            S.y[1] = df_from_double(theta);
+            S.y[2] = df_from_double(psi0);
+            for (int k = 0; k < 3; k++) S.muf[k] = DF_ADD(S.mu[k].hi, S.mu[k].lo);
+            S.muf[3] = (float)DD_SUB(1.0, Ip);
+        }
+    }
+    S.bw = (flags & AST_BW_BALL) != 0;
+    float b_ph = 1, c_ph = 1;
+    F.kappa = F.cos_phR = F.sin_phR = F.cos_thR = F.sin_thR = 0;
+    if (S.bw) {
+        F.kappa = (float)AST_P(kappa);
+        sincosf((float)AST_P(phi_R), &F.sin_phR, &F.cos_phR);
+        sincosf((float)AST_P(theta_R), &F.sin_thR, &F.cos_thR);
+    } else {
+        b_ph = (float)((flags & AST_BC) ? AST_P(b) : bt);
+        c_ph = (float)((flags & AST_BC) ? AST_P(c) : ct);
+    }
+    F.ib = 1.0f / b_ph;
+    F.ic = 1.0f / c_ph;
+    F.bc = DF_MUL(b_ph, c_ph);
+#undef AST_P
+}
+
+// Integrate from observation i-1 to i (cuda.c:319-372; nothing for i = 0) and return the Euler
+// angles (phi, theta, psi) reduced to [-pi, pi].  They enter the right-hand side and the
+// brightness only through sin and cos, so the state itself is kept reduced: the double-float then
+// resolves the phase to ~1e-14 rad instead of u^2 of the accumulated angle.  RHS32: the FP32
+// right-hand side (AST_PREC_MIXED_RHS32), a separate instantiation so that the double-float
+// kernels carry none of its code.
+template <bool RHS32>
+AST_HD void mixed_advance(MixedState& S, const ObsView& o, int i, const float4* tab, df* ang)
+{
+    if (i > 0) {
+        const int N_steps = o.nst[i];
+        const float4 hq = o.hq[i], hw = o.hw[i];
+        // Not unrolled: one copy of the step keeps the hot loop inside the instruction cache.
+        if (RHS32) {
+            if (S.torque) {
+#pragma unroll 1
+                for (int l = 0; l < N_steps; l++) rk4_step_f32<6>(S.y, hq, hw, S.muf, tab);
+            } else {
+#pragma unroll 1
+                for (int l = 0; l < N_steps; l++) rk4_step_f32<3>(S.y, hq, hw, S.muf, tab);
+            }
+        } else if (S.torque) {
+#pragma unroll 1
+            for (int l = 0; l < N_steps; l++) rk4_step_df<6>(S.y, hq, hw, S.mu, tab);
+        } else {
+#pragma unroll 1
+            for (int l = 0; l < N_steps; l++) rk4_step_df<3>(S.y, hq, hw, S.mu, tab);
+        }
+    }
+    // (Constant indices only: an index computed at run time would move y to local memory.)
+    if (S.torque) {
+        S.y[3] = df_reduce_2pi(S.y[3]);
+        S.y[4] = df_reduce_2pi(S.y[4]);
+        S.y[5] = df_reduce_2pi(S.y[5]);
+        ang[0] = S.y[3];
+        ang[1] = S.y[4];
+        ang[2] = S.y[5];
+    } else {
+        S.y[0] = df_reduce_2pi(S.y[0]);
+        S.y[1] = df_reduce_2pi(S.y[1]);
+        S.y[2] = df_reduce_2pi(S.y[2]);
+        ang[0] = S.y[0];
+        ang[1] = S.y[1];
+        ang[2] = S.y[2];
+    }
+}
+
+// FP32 model magnitude at observation i for the Euler angles (phi, theta, psi): the body frame
+// as in cuda.c:432-473, then the cancellation-free Lommel-Seeliger form (ls_magnitude_f) or the
+// BW_BALL law (cuda.c:475-497, 603-607).
+AST_HD float mixed_vmod(const MixedFrame& F, bool bw, float phi, float theta, float psi, const ObsView& o, int i)
+{
+    float sin_phi, cos_phi, sin_theta, cos_theta, sin_psi, cos_psi;
+    sincosf(phi, &sin_phi, &cos_phi);
+    sincosf(theta, &sin_theta, &cos_theta);
+    sincosf(psi, &sin_psi, &cos_psi);
+    float N_x = f_dot2(F.XM_x, cos_phi, F.YM_x, sin_phi);
+    float N_y = DF_MUL(F.YM_y, sin_phi);
+    float N_z = f_dot2(F.XM_z, cos_phi, F.YM_z, sin_phi);
+    float p_x = f_dif2(N_y, F.M_z, N_z, F.M_y);
+    float p_y = f_dif2(N_z, F.M_x, N_x, F.M_z);
+    float p_z = f_dif2(N_x, F.M_y, N_y, F.M_x);
+    float a_x = f_dot2(F.M_x, cos_theta, p_x, sin_theta);
+    float a_y = f_dot2(F.M_y, cos_theta, p_y, sin_theta);
+    float a_z = f_dot2(F.M_z, cos_theta, p_z, sin_theta);
+    const float w_x = f_dif2(a_y, N_z, a_z, N_y);
+    const float w_y = f_dif2(a_z, N_x, a_x, N_z);
+    const float w_z = f_dif2(a_x, N_y, a_y, N_x);
+    const float b_x = f_dot2(N_x, cos_psi, w_x, sin_psi);
+    const float b_y = f_dot2(N_y, cos_psi, w_y, sin_psi);
+    const float b_z = f_dot2(N_z, cos_psi, w_z, sin_psi);
+    const float c_x = f_dif2(a_y, b_z, a_z, b_y);
+    const float c_y = f_dif2(a_z, b_x, a_x, b_z);
+    const float c_z = f_dif2(a_x, b_y, a_y, b_x);
+    const float E_x1 = o.efx[i], E_y1 = o.efy[i], E_z1 = o.efz[i];
+    const float S_x1 = o.sfx[i], S_y1 = o.sfy[i], S_z1 = o.sfz[i];
+    if (bw) {
+        N_x = f_dot2(b_x, F.cos_phR, c_x, F.sin_phR);
+        N_y = f_dot2(b_y, F.cos_phR, c_y, F.sin_phR);
+        N_z = f_dot2(b_z, F.cos_phR, c_z, F.sin_phR);
+        p_x = f_dif2(N_y, a_z, N_z, a_y);
+        p_y = f_dif2(N_z, a_x, N_x, a_z);
+        p_z = f_dif2(N_x, a_y, N_y, a_x);
+        a_x = f_dot2(a_x, F.cos_thR, p_x, F.sin_thR);
+        a_y = f_dot2(a_y, F.cos_thR, p_y, F.sin_thR);
+        a_z = f_dot2(a_z, F.cos_thR, p_z, F.sin_thR);
+        const float cos_zeta = f_dot3(a_x, E_x1, a_y, E_y1, a_z, E_z1);
+        const float arg = f_dot2(F.kappa, DF_ADD(1.0f, cos_zeta), 0.5f, DF_SUB(1.0f, cos_zeta));
+        return DF_MUL(-2.5f, log10f(DF_MUL(0.5f, arg)));
+    }
+    const float Ep_b = f_dot3(b_x, E_x1, b_y, E_y1, b_z, E_z1);
+    const float Ep_c = f_dot3(c_x, E_x1, c_y, E_y1, c_z, E_z1);
+    const float Ep_a = f_dot3(a_x, E_x1, a_y, E_y1, a_z, E_z1);
+    const float Sp_b = f_dot3(b_x, S_x1, b_y, S_y1, b_z, S_z1);
+    const float Sp_c = f_dot3(c_x, S_x1, c_y, S_y1, c_z, S_z1);
+    const float Sp_a = f_dot3(a_x, S_x1, a_y, S_y1, a_z, S_z1);
+    return ls_magnitude_f(Sp_b, Sp_c, Sp_a, Ep_b, Ep_c, Ep_a, F.ib, F.ic, F.bc);
+}
+
 // Same contract as chi2_fp64 (model.cuh); tab is the shared-memory sin/cos table; ang_out, when
-// non-null, receives the Euler angles at every observation (reduced to [-pi, pi]).
-template <class CF>
+// non-null, receives the Euler angles at every observation (reduced to [-pi, pi]).  RHS32 selects
+// the FP32 right-hand side of AST_PREC_MIXED_RHS32.
+template <class CF, bool RHS32 = false>
 __host__ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const double* params, CF* delta_V, const float4* tab,
                                   double* ang_out = nullptr)
 {
     const int flags = M.flags;
-    const ast_type_ids& T = M.t;
     const int N_data = M.n_data, N_filters = M.n_filters;
     df sum_y2[AST_MAX_FILTERS], sum_y[AST_MAX_FILTERS];
     for (int m = 0; m < N_filters; m++) { sum_y2[m] = df{0.0f, 0.0f}; sum_y[m] = df{0.0f, 0.0f}; }
@@ -440,162 +633,17 @@ __host__ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const dou
     df ang_old[2][3] = {};
     NudgeCand cand[kNudgeQueue];
     int n_cand = 0;
-
-#define AST_P(tt) params[M.idx[T.tt]]
-    // Per-evaluation set-up in FP64.
-    const double th_M = AST_P(theta_M), ph_M = AST_P(phi_M);
-    // Every rounding explicit (DD_*, DF_*, f_*, d_*), with float and double operands as in the
-    // reference's expressions: the same bits in every kernel that inlines this function.
-    const double M_xd = DD_MUL(sin(th_M), cos(ph_M)), M_yd = DD_MUL(sin(th_M), sin(ph_M)), M_zd = cos(th_M);
-    const double XMd = sqrt(d_dot2(M_zd, M_zd, M_xd, M_xd));
-    const float M_x = (float)M_xd, M_y = (float)M_yd, M_z = (float)M_zd;
-    const float XM_x = (float)(M_zd / XMd), XM_z = (float)(-M_xd / XMd);
-    const float YM_x = DF_MUL(M_y, XM_z), YM_y = f_dif2(M_z, XM_x, M_x, XM_z), YM_z = -DF_MUL(M_y, XM_x);
-    const double bt = AST_P(b_tumb), ct = AST_P(c_tumb);
-    const double bt2 = DD_MUL(bt, bt), ct2 = DD_MUL(ct, ct);
-    const double Is = DD_ADD(1.0, bt2) / DD_ADD(bt2, ct2);
-    const double Ii = DD_ADD(1.0, ct2) / DD_ADD(bt2, ct2);
-    const double Is_inv = 1.0 / Is, Ii_inv = 1.0 / Ii;
-    const double psi0 = AST_P(psi_0);
-    df y[6];
-    df mu[6];
-    float muf[6];  // the same constants in FP32 for the FP32 right-hand side
-    const bool torque = (flags & AST_TORQUE) != 0;
-    const bool rhs32 = (flags & kFlagRhs32) != 0;
-    {
-        const double sp = sin(psi0);
-        const double den = DD_SUB(DD_ADD(DD_MUL(DD_MUL(sp, sp), DD_SUB(Ii_inv, Is_inv)), Is_inv), 1.0);
-        const double theta = asin(sqrt(DD_SUB(AST_P(Es), 1.0) / den));
-        if (torque) {
-            mu[0] = df_from_double(DD_MUL(DD_SUB(Is, 1.0), Ii_inv));
-            mu[1] = df_from_double(DD_MUL(DD_SUB(1.0, Ii), Is_inv));
-            mu[2] = df_from_double(DD_SUB(Ii, Is));
-            mu[3] = df_from_double(AST_P(Ti));
-            mu[4] = df_from_double(AST_P(Ts));
-            mu[5] = df_from_double(AST_P(Tl));
-            const double L = AST_P(L);
-            y[0] = df_from_double(DD_MUL(DD_MUL(DD_MUL(L, Ii_inv), sin(theta)), sp));
-            y[1] = df_from_double(DD_MUL(DD_MUL(DD_MUL(L, Is_inv), sin(theta)), cos(psi0)));
-            y[2] = df_from_double(DD_MUL(L, cos(theta)));
-            y[3] = df_from_double(AST_P(phi_0));
-            y[4] = df_from_double(theta);
-            y[5] = df_from_double(psi0);
-            for (int k = 0; k < 6; k++) muf[k] = DF_ADD(mu[k].hi, mu[k].lo);
-        } else {
-            mu[0] = df_from_double(AST_P(L));
-            const double Ip = DD_MUL(0.5, DD_ADD(Ii_inv, Is_inv));
-            mu[1] = df_from_double(Ip);
-            mu[2] = df_from_double(DD_MUL(0.5, DD_SUB(Ii_inv, Is_inv)));
-            y[0] = df_from_double(AST_P(phi_0));
-            y[1] = df_from_double(theta);
-            y[2] = df_from_double(psi0);
-            for (int k = 0; k < 3; k++) muf[k] = DF_ADD(mu[k].hi, mu[k].lo);
-            muf[3] = (float)DD_SUB(1.0, Ip);
-        }
-    }
-    const bool bw = (flags & AST_BW_BALL) != 0;
-    float b_ph = 1, c_ph = 1, kappa = 0, cos_phR = 0, sin_phR = 0, cos_thR = 0, sin_thR = 0;
-    if (bw) {
-        kappa = (float)AST_P(kappa);
-        sincosf((float)AST_P(phi_R), &sin_phR, &cos_phR);
-        sincosf((float)AST_P(theta_R), &sin_thR, &cos_thR);
-    } else {
-        b_ph = (float)((flags & AST_BC) ? AST_P(b) : bt);
-        c_ph = (float)((flags & AST_BC) ? AST_P(c) : ct);
-    }
-    const float ib = 1.0f / b_ph, ic = 1.0f / c_ph;
+    MixedState S;
+    mixed_setup(M, params, S);
     DfFrame F;
     if (flags & AST_NUDGE) F = make_df_frame(M, params);
     for (int i = 0; i < N_data; i++) {
-        if (i > 0) {
-            const int N_steps = o.nst[i];
-            const float4 hq = o.hq[i], hw = o.hw[i];
-            // Not unrolled: one copy of the step keeps the hot loop inside the instruction cache.
-            if (rhs32) {
-                if (torque) {
-#pragma unroll 1
-                    for (int l = 0; l < N_steps; l++) rk4_step_f32<6>(y, hq, hw, muf, tab);
-                } else {
-#pragma unroll 1
-                    for (int l = 0; l < N_steps; l++) rk4_step_f32<3>(y, hq, hw, muf, tab);
-                }
-            } else if (torque) {
-#pragma unroll 1
-                for (int l = 0; l < N_steps; l++) rk4_step_df<6>(y, hq, hw, mu, tab);
-            } else {
-#pragma unroll 1
-                for (int l = 0; l < N_steps; l++) rk4_step_df<3>(y, hq, hw, mu, tab);
-            }
-        }
-        // The Euler angles enter the right-hand side and the brightness only through sin and
-        // cos, so they are kept reduced to [-pi, pi]: the double-float then resolves the phase
-        // to ~1e-14 rad instead of u^2 of the accumulated angle.
-        // (Constant indices only: an index computed at run time would move y to local memory.)
         df ang[3];
-        if (torque) {
-            y[3] = df_reduce_2pi(y[3]);
-            y[4] = df_reduce_2pi(y[4]);
-            y[5] = df_reduce_2pi(y[5]);
-            ang[0] = y[3];
-            ang[1] = y[4];
-            ang[2] = y[5];
-        } else {
-            y[0] = df_reduce_2pi(y[0]);
-            y[1] = df_reduce_2pi(y[1]);
-            y[2] = df_reduce_2pi(y[2]);
-            ang[0] = y[0];
-            ang[1] = y[1];
-            ang[2] = y[2];
-        }
+        mixed_advance<RHS32>(S, o, i, tab, ang);
         if (ang_out)
             for (int k = 0; k < 3; k++) ang_out[3 * i + k] = df_to_double(ang[k]);
-        float sin_phi, cos_phi, sin_theta, cos_theta, sin_psi, cos_psi;
-        sincosf(DF_ADD(ang[0].hi, ang[0].lo), &sin_phi, &cos_phi);
-        sincosf(DF_ADD(ang[1].hi, ang[1].lo), &sin_theta, &cos_theta);
-        sincosf(DF_ADD(ang[2].hi, ang[2].lo), &sin_psi, &cos_psi);
-        float N_x = f_dot2(XM_x, cos_phi, YM_x, sin_phi);
-        float N_y = DF_MUL(YM_y, sin_phi);
-        float N_z = f_dot2(XM_z, cos_phi, YM_z, sin_phi);
-        float p_x = f_dif2(N_y, M_z, N_z, M_y);
-        float p_y = f_dif2(N_z, M_x, N_x, M_z);
-        float p_z = f_dif2(N_x, M_y, N_y, M_x);
-        float a_x = f_dot2(M_x, cos_theta, p_x, sin_theta);
-        float a_y = f_dot2(M_y, cos_theta, p_y, sin_theta);
-        float a_z = f_dot2(M_z, cos_theta, p_z, sin_theta);
-        const float w_x = f_dif2(a_y, N_z, a_z, N_y);
-        const float w_y = f_dif2(a_z, N_x, a_x, N_z);
-        const float w_z = f_dif2(a_x, N_y, a_y, N_x);
-        const float b_x = f_dot2(N_x, cos_psi, w_x, sin_psi);
-        const float b_y = f_dot2(N_y, cos_psi, w_y, sin_psi);
-        const float b_z = f_dot2(N_z, cos_psi, w_z, sin_psi);
-        const float c_x = f_dif2(a_y, b_z, a_z, b_y);
-        const float c_y = f_dif2(a_z, b_x, a_x, b_z);
-        const float c_z = f_dif2(a_x, b_y, a_y, b_x);
-        const float E_x1 = o.efx[i], E_y1 = o.efy[i], E_z1 = o.efz[i];
-        const float S_x1 = o.sfx[i], S_y1 = o.sfy[i], S_z1 = o.sfz[i];
-        float Vmod;
-        if (bw) {
-            N_x = f_dot2(b_x, cos_phR, c_x, sin_phR);
-            N_y = f_dot2(b_y, cos_phR, c_y, sin_phR);
-            N_z = f_dot2(b_z, cos_phR, c_z, sin_phR);
-            p_x = f_dif2(N_y, a_z, N_z, a_y);
-            p_y = f_dif2(N_z, a_x, N_x, a_z);
-            p_z = f_dif2(N_x, a_y, N_y, a_x);
-            a_x = f_dot2(a_x, cos_thR, p_x, sin_thR);
-            a_y = f_dot2(a_y, cos_thR, p_y, sin_thR);
-            a_z = f_dot2(a_z, cos_thR, p_z, sin_thR);
-            const float cos_zeta = f_dot3(a_x, E_x1, a_y, E_y1, a_z, E_z1);
-            const float arg = f_dot2(kappa, DF_ADD(1.0f, cos_zeta), 0.5f, DF_SUB(1.0f, cos_zeta));
-            Vmod = DF_MUL(-2.5f, log10f(DF_MUL(0.5f, arg)));
-        } else {
-            const float Ep_b = f_dot3(b_x, E_x1, b_y, E_y1, b_z, E_z1);
-            const float Ep_c = f_dot3(c_x, E_x1, c_y, E_y1, c_z, E_z1);
-            const float Ep_a = f_dot3(a_x, E_x1, a_y, E_y1, a_z, E_z1);
-            const float Sp_b = f_dot3(b_x, S_x1, b_y, S_y1, b_z, S_z1);
-            const float Sp_c = f_dot3(c_x, S_x1, c_y, S_y1, c_z, S_z1);
-            const float Sp_a = f_dot3(a_x, S_x1, a_y, S_y1, a_z, S_z1);
-            Vmod = ls_magnitude_f(Sp_b, Sp_c, Sp_a, Ep_b, Ep_c, Ep_a, ib, ic, DF_MUL(b_ph, c_ph));
-        }
+        const float Vmod = mixed_vmod(S.F, S.bw, DF_ADD(ang[0].hi, ang[0].lo), DF_ADD(ang[1].hi, ang[1].lo),
+                                      DF_ADD(ang[2].hi, ang[2].lo), o, i);
         {
             // Residual and weighted sums as double-floats: v - Vmod exactly (TwoSum), products
             // to ~u^2, sums with the sloppy double-float add (absolute error ~u^2 of the sum).
@@ -641,7 +689,6 @@ __host__ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const dou
         }
     }
     if ((flags & AST_NUDGE) && !nudge_flush(M, o, F, tab, cand, &n_cand, &Mmin, t_mod, V_mod)) return (CF)kHuge;
-#undef AST_P
     CF chi2m, chi2a = 0.0, SUM_w = 0.0;
     CF dv[AST_MAX_FILTERS];
     for (int m = 0; m < N_filters; m++) {

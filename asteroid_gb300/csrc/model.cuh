@@ -21,9 +21,7 @@ namespace ast {
 
 constexpr double kPi = 3.141592653589793238;
 constexpr double kHuge = 1e30;
-// DevModel.flags bit outside the public AST_* variant flags: the mixed path evaluates the
-// right-hand side of the rotation ODEs in FP32 (AST_PREC_MIXED_RHS32).
-constexpr int32_t kFlagRhs32 = 1 << 20;
+
 
 // Tables of one variant, by value in kernel parameters (the reference's dProperty, dTypes,
 // dLimits, d_x2_params, d_chi2_params symbols, asteroid.h:460,509-513,533).
@@ -52,8 +50,8 @@ struct DevModel {
 // one CTA of 256 threads with the full register file.
 template <int PREC>
 struct KernShape {
-    static constexpr int tpb = PREC == AST_PREC_MIXED ? 128 : 256;
-    static constexpr int min_ctas = PREC == AST_PREC_MIXED ? 3 : 1;
+    static constexpr int tpb = PREC != AST_PREC_FP64 ? 128 : 256;
+    static constexpr int min_ctas = PREC != AST_PREC_FP64 ? 3 : 1;
 };
 
 // SoA observations of one object (one device buffer; also the shared-memory image).

@@ -137,7 +137,7 @@ __device__ __forceinline__ CF eval_point(const DevModel& M, const ObsView& o, co
                                          const float4* trig)
 {
     if (PREC == AST_PREC_FP64) return chi2_fp64<CF>(M, o, params, dv);
-    return chi2_mixed<CF>(M, o, params, dv, trig);
+    return chi2_mixed<CF, PREC == AST_PREC_MIXED_RHS32>(M, o, params, dv, trig);
 }
 
 // Register state of a slot between evaluations.
@@ -224,23 +224,16 @@ __device__ __forceinline__ void nm_finish(const DevModel& M, const FitView<CF>& 
     n_fit += V.last_stage ? 1 : 0;
 }
 
-// One evaluation of the slot's chain and the simplex move it completes (cuda.c:1546-1760),
-// as a state machine: INIT evaluates the N+1 start vertices, then REFLECT / EXPAND / CONTRACT /
-// SHRINK.  V carries the slot buffers and the chain-level settings of the chain's object.
-// Returns true when the chain has finished (its result is written).
-template <class CF, int PREC>
-__device__ __forceinline__ bool slot_iterate(const DevModel& M, const ObsView& o, const FitView<CF>& V, int64_t s,
-                                             SlotState<CF>& R, const float4* trig, unsigned long long& n_ev,
-                                             unsigned long long& n_fit)
+// The point the slot's chain evaluates next, in x (cuda.c:1512-1545 start vertices, 1635-1640
+// reflection, 1660-1663 expansion, 1694-1698 contraction, 1716-1722 shrink).
+template <class CF>
+__device__ __forceinline__ void slot_point(const DevModel& M, const FitView<CF>& V, int64_t s, const SlotState<CF>& R,
+                                           CF* p)
 {
     const int N = M.n_params;
     const int64_t S = V.S;
-    const CF HUGEV = (CF)kHuge;
-    int32_t st = R.st;
-    const int phase = st & 0xff;
-    int j = (st >> 8) & 0xff;
-    int bad = (st >> 16) & 1;
-    CF p[AST_MAX_PARAMS];
+    const int phase = R.st & 0xff;
+    const int j = (R.st >> 8) & 0xff;
     if (phase == PH_INIT) {
         for (int i = 0; i < N; i++) p[i] = XV(j, i);
     } else if (phase == PH_REFLECT || phase == PH_CONTRACT) {
@@ -254,15 +247,23 @@ __device__ __forceinline__ bool slot_iterate(const DevModel& M, const ObsView& o
         const int v = IND(j);
         for (int i = 0; i < N; i++) p[i] = XV(v, i);
     }
-    // One evaluation: x -> params (hard limits), then chi^2.
-    double params[AST_MAX_PARAMS];
-    const int rej = x2params<CF>(M, V.reopt, p, params);
-    CF fv = HUGEV;
-    if (!rej) {
-        fv = eval_point<CF, PREC>(M, o, params, R.dvl, trig);
-        R.ev++;
-        n_ev++;
-    }
+}
+
+// The simplex move an evaluation completes (cuda.c:1546-1760), as a state machine: INIT
+// evaluates the N+1 start vertices, then REFLECT / EXPAND / CONTRACT / SHRINK.  p is the point
+// slot_point gave, rej whether x2params rejected it, fv its chi^2 (counted in R.ev by the
+// caller).  Returns true when the chain has finished (its result is written).
+template <class CF>
+__device__ __forceinline__ bool slot_apply(const DevModel& M, const FitView<CF>& V, int64_t s, SlotState<CF>& R,
+                                           const CF* p, int rej, CF fv, unsigned long long& n_fit)
+{
+    const int N = M.n_params;
+    const int64_t S = V.S;
+    const CF HUGEV = (CF)kHuge;
+    int32_t st = R.st;
+    const int phase = st & 0xff;
+    int j = (st >> 8) & 0xff;
+    int bad = (st >> 16) & 1;
     bool iter_top = false, finish = false, failed = false;
     if (phase == PH_INIT) {
         if (rej) {
@@ -335,6 +336,28 @@ __device__ __forceinline__ bool slot_iterate(const DevModel& M, const ObsView& o
     R.st = st;
     if (finish) nm_finish<CF>(M, V, s, R, failed, n_fit);
     return finish;
+}
+
+// One evaluation of the slot's chain and the simplex move it completes.  V carries the slot
+// buffers and the chain-level settings of the chain's object.  Returns true when the chain has
+// finished (its result is written).
+template <class CF, int PREC>
+__device__ __forceinline__ bool slot_iterate(const DevModel& M, const ObsView& o, const FitView<CF>& V, int64_t s,
+                                             SlotState<CF>& R, const float4* trig, unsigned long long& n_ev,
+                                             unsigned long long& n_fit)
+{
+    CF p[AST_MAX_PARAMS];
+    slot_point<CF>(M, V, s, R, p);
+    // One evaluation: x -> params (hard limits), then chi^2.
+    double params[AST_MAX_PARAMS];
+    const int rej = x2params<CF>(M, V.reopt, p, params);
+    CF fv = (CF)kHuge;
+    if (!rej) {
+        fv = eval_point<CF, PREC>(M, o, params, R.dvl, trig);
+        R.ev++;
+        n_ev++;
+    }
+    return slot_apply<CF>(M, V, s, R, p, rej, fv, n_fit);
 }
 
 

@@ -145,10 +145,10 @@ double h_vmod_diff(const ast_model* m, const ast_obs_set* obs, const double* par
 double h_chi2_mixed_rhs(const ast_model* m, const ast_obs_set* obs, const double* params, double* dv, int rhs32)
 {
     Block B = prepare(m, obs);
-    if (rhs32) B.dm.flags |= kFlagRhs32;
     const std::vector<float4> tab = table();
     double d[AST_MAX_FILTERS];
-    const double r = chi2_mixed<double>(B.dm, B.o, params, d, tab.data());
+    const double r = rhs32 ? chi2_mixed<double, true>(B.dm, B.o, params, d, tab.data())
+                           : chi2_mixed<double, false>(B.dm, B.o, params, d, tab.data());
     for (int k = 0; k < obs->n_filters; k++) dv[k] = d[k];
     return r;
 }

@@ -14,12 +14,21 @@ distribution of outcomes.  At each seed, on 4096 chains per side, the test requi
     compared separately: their fractions within 4 standard errors);
   * the 10/50/90% quantiles of one side to sit at the same quantile of the other side within
     4 standard errors of an empirical quantile, sqrt(p(1-p)(1/n1 + 1/n2));
-  * KS p > 1e-3 for the group bests (groups of 32 chains, the reference's block best);
+  * KS p > 1e-3 for the group bests (the reference's block bests; groups of 4 chains);
   * evaluations per chain within 5% of each other.
-The same checks are pooled over the seeds at the end.  The chain count and group size are the
-reference's N_BLOCKS x BSIZE = 4096 chains run as 128 blocks of 32 threads: with one stage a
-chain's outcome does not depend on its block, and 128 blocks spread over 128 SMs instead of 16.
+The same checks are pooled over the seeds at the end.
+
+Sizes.  4096 chains, the config-0 chain count.  With one stage a chain's outcome does not
+depend on its block, so the reference's chains run as 1024 blocks of 4 threads and the groups
+(block bests) here are groups of 4: one FP64 warp per SM is latency-bound on this GPU (about
+200 ms per reference chi2one of this object with a single warp), and the reference kernel's 30 KB
+of static shared memory allows at most 7 blocks per SM, so small blocks are what spreads its
+chains over the SMs.  The iteration cap is N_STEPS = 100 (about 160 evaluations per chain):
+config 0's 2000 evaluations per chain take the reference kernel about two minutes per seed even
+so.  AST_REF_SIMPLEX_STEPS sets another cap for a longer run.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -28,8 +37,8 @@ from asteroid_gb300 import api
 pytestmark = pytest.mark.gpu
 
 N_CHAINS = 4096
-BLOCK = 32
-N_STEPS = 1500      # simplex iterations per chain (about 2000 evaluations, config 0's count)
+BLOCK = 4
+N_STEPS = int(os.environ.get("AST_REF_SIMPLEX_STEPS", "100"))  # simplex iterations per chain
 SEEDS = (101, 202)
 P_MIN = 1e-3
 FAILED = 1e29
