@@ -178,8 +178,6 @@ def build_reference_oracle() -> None:
             _run(["bash", str(script)])
         elif not (ORACLE / "_ref" / "libref_minima.so").exists():
             _run(["bash", str(script), "minima"])
-        if not (ORACLE / "_ref" / "ref_nm_ppsi_torque_acc.cubin").exists():
-            _run(["bash", str(script), "nm"])
         if not (ORACLE / "_ref" / "ref_ppsi_torque_acc_nofma.cubin").exists():
             _run(["bash", str(script), "nofma"])
 

@@ -14,10 +14,6 @@
 #                        oracle/ref_harness_animate.cu: the reference's compute_rgb on the GPU.
 #   ref_<variant>_nofma.cubin  the same device build with nvcc -fmad=false (no multiply-add
 #                        contraction), for the parity check against the engine built the same way.
-#   ref_nm_<variant>.cubin  device build (sm_100) of cuda.c whose setup_kernel + chi2_gpu
-#                        (cuda.c:2039,1326) run on the GPU through refn_fit in
-#                        oracle/ref_gpu_loader.cpp; three instrumentation hooks are inserted in
-#                        the stream (oracle/ref_harness_nm_pre.cuh says which), nothing else.
 #
 # The reference's asteroid.h and cuda.c are streamed through sed into nvcc's standard input:
 # the four device functions become __host__ __device__ (host build only), N_FILTERS becomes 8
@@ -83,31 +79,6 @@ if [[ "${1:-all}" == "all" || "${1:-all}" == "cubin" || "${1:-all}" == "animate"
       nvcc -x cu -cubin -arch=sm_100 -O3 -DMAIN -DANIMATE -I"$REF" -w -o "$OUT/ref_animate.cubin" - ) &
     pids+=($!)
 fi
-# Simplex builds: N_STEPS becomes a device variable, chi2one counts its calls, chi2_gpu records
-# every chain's final chi^2 after each stage.
-NM_VARIANTS=(
-  "ppsi_torque_acc 1e-2 -DP_PSI -DTORQUE -DACC"
-)
-stream_nm_source() {  # $1 = time step
-    sed -e 's/^const int N_FILTERS = 1;/const int N_FILTERS = 8;/' \
-        -e "s/^const double TIME_STEP = 1e-2;.*/const double TIME_STEP = $1;/" \
-        -e 's/^const unsigned int N_STEPS = 5000;.*/extern __device__ unsigned int refk_n_steps;\n#define N_STEPS refk_n_steps/' \
-        "$REF/asteroid.h"
-    cat "$here/ref_harness_nm_pre.cuh"
-    sed -e 's/^#include "asteroid.h"//' \
-        -e '/^\/\/ Computung chi^2 for a single model parameters combination, on GPU, by a single thread$/{n;n;s/^{$/{ refk_count_eval();/;}' \
-        -e 's|^    //!!! AT this point not all warps initialized s_f and s_thread_id!.*$|    refk_record_chain(id, istage, (double)s_f[threadIdx.x], l);|' \
-        "$REF/cuda.c"
-    cat "$here/ref_harness_kernel.cu" "$here/ref_harness_nm.cu"
-}
-if [[ "${1:-all}" == "all" || "${1:-all}" == "cubin" || "${1:-all}" == "nm" ]]; then
-    for v in "${NM_VARIANTS[@]}"; do
-        read -r name ts macros <<<"$v"
-        ( stream_nm_source "$ts" | nvcc -x cu -cubin -arch=sm_100 -O3 -DMAIN $macros -I"$REF" -w \
-              -o "$OUT/ref_nm_$name.cubin" - ) &
-        pids+=($!)
-    done
-fi
 if [[ "${1:-all}" == "all" || "${1:-all}" == "cubin" || "${1:-all}" == "nofma" ]]; then
     for v in "${VARIANTS[@]}"; do
         read -r name ts macros <<<"$v"
@@ -116,7 +87,7 @@ if [[ "${1:-all}" == "all" || "${1:-all}" == "cubin" || "${1:-all}" == "nofma" ]
         pids+=($!)
     done
 fi
-[[ "${1:-all}" == "minima" || "${1:-all}" == "animate" || "${1:-all}" == "nm" || "${1:-all}" == "nofma" ]] && VARIANTS=()
+[[ "${1:-all}" == "minima" || "${1:-all}" == "animate" || "${1:-all}" == "nofma" ]] && VARIANTS=()
 for v in "${VARIANTS[@]}"; do
     read -r name ts macros <<<"$v"
     if [[ "${1:-all}" == "all" || "${1:-all}" == "host" ]]; then

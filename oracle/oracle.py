@@ -282,59 +282,6 @@ class RefHost:
         return x
 
 
-class RefSimplex:
-    """The reference's own setup_kernel + chi2_gpu on the GPU (oracle/_ref/ref_nm_<variant>.cubin,
-    sm_100): one fitting pass of n_blocks x block chains, with the per-chain records of the
-    instrumentation hooks (oracle/ref_harness_nm_pre.cuh)."""
-
-    DV_STRIDE = 8  # N_FILTERS of the reference builds (build_ref.sh)
-
-    def __init__(self, variant: str):
-        self.cubin = REF_DIR / f"ref_nm_{variant}.cubin"
-        if not self.cubin.exists():
-            raise FileNotFoundError(self.cubin)
-        lib = C.CDLL(str(HERE / "_build" / "libref_gpu_loader.so"))
-        lib.refn_fit.restype = C.c_int
-        lib.refk_last_error.restype = C.c_char_p
-        self.lib = lib
-
-    def fit(self, model, obs, seed, n_blocks, block, n_stages=1, n_steps=5000, reopt=False, params0=None):
-        prop = np.ctypeslib.as_array(model.property).reshape(-1, 6)[: model.n_params].astype(np.int32).copy()
-        lim = np.ctypeslib.as_array(model.limits).reshape(2, -1).astype(np.float64).copy()
-        max_types = lim.shape[1]
-        types = np.zeros(max_types, np.int32)
-        types[: model.n_types] = np.ctypeslib.as_array(model.types)[: model.n_types]
-        eph = np.concatenate([np.asarray(obs.eph_e).ravel(), np.asarray(obs.eph_s).ravel(),
-                              np.asarray(obs.eph_mjd0).ravel()]).astype(np.float64)
-        T = n_blocks * block
-        N = model.n_params
-        sizes = np.zeros(5, np.int32)
-        bf = np.zeros(n_blocks)
-        bp = np.zeros((n_blocks, N))
-        bdv = np.zeros((n_blocks, self.DV_STRIDE))
-        cf = np.zeros((n_stages, T))
-        cl = np.zeros((n_stages, T), np.int32)
-        ev = np.zeros(T, np.uint32)
-        ms = C.c_double(0)
-        p0 = None if params0 is None else np.ascontiguousarray(params0, dtype=np.float64)
-        V = C.c_void_p
-        rc = self.lib.refn_fit(
-            str(self.cubin).encode(), V(prop.ctypes.data), V(types.ctypes.data), V(lim.ctypes.data), max_types,
-            C.c_float(model.ppsi1), C.c_float(model.ppsi2), obs.n_data, obs.n_filters, V(obs.mjd.ctypes.data),
-            V(obs.v.ctypes.data), V(obs.w.ctypes.data), V(obs.filt.ctypes.data), V(obs.e_unit.ctypes.data),
-            V(obs.s_unit.ctypes.data), V(eph.ctypes.data), int(obs.t_min.size), V(obs.t_min.ctypes.data),
-            V(obs.v_min.ctypes.data), C.c_uint64(seed), int(n_blocks), int(block), int(n_stages), int(bool(reopt)),
-            V(p0.ctypes.data) if p0 is not None else None, C.c_uint(n_steps), V(sizes.ctypes.data),
-            V(bf.ctypes.data), V(bp.ctypes.data), V(bdv.ctypes.data), self.DV_STRIDE, V(cf.ctypes.data),
-            V(cl.ctypes.data), V(ev.ctypes.data), C.byref(ms))
-        if rc:
-            raise RuntimeError(self.lib.refk_last_error().decode())
-        if sizes[3] != N:
-            raise RuntimeError(f"cubin has N_PARAMS {sizes[3]}, the model {N}")
-        return {"best_f": bf, "best_params": bp, "best_dv": bdv[:, : obs.n_filters], "chain_f": cf,
-                "chain_l": cl, "evals": ev, "kernel_ms": ms.value}
-
-
 def ref_render(geo):
     """The reference's own compute_rgb on the GPU (oracle/_ref/ref_animate.cubin), 1080 x 1080."""
     cubin = REF_DIR / "ref_animate.cubin"
