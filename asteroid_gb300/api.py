@@ -516,16 +516,24 @@ class Batch:
     def tune(self, evals_per_slot=4) -> dict:
         t = capi.BatchTune()
         check(self.lib.ast_batch_tune(self.h, int(evals_per_slot), C.byref(t)), "ast_batch_tune")
-        return dict(tpb=t.tpb, refill=t.refill, ctas=t.ctas, evals_per_s=t.evals_per_s)
+        return dict(tpb=t.tpb, refill=t.refill, ctas=t.ctas, evals_per_s=t.evals_per_s, tile=t.tile)
 
-    def run(self, tpb=0, refill=0) -> float:
+    def run(self, tpb=0, refill=0, tile=0) -> float:
+        """Every chain to completion in one graph-captured launch; tpb / refill / tile set the
+        geometry (0: the tuned or default one).  Returns the device milliseconds."""
         ms = C.c_double(0)
         t = None
         if tpb:
             t = capi.BatchTune()
-            t.tpb, t.refill = int(tpb), int(refill or 1)
+            t.tpb, t.refill, t.tile = int(tpb), int(refill or 1), int(tile)
         check(self.lib.ast_batch_run(self.h, C.byref(t) if t is not None else None, C.byref(ms)), "ast_batch_run")
         return ms.value
+
+    def set_geometry(self, tpb, refill=1, tile=0):
+        """The launch geometry of the following step() calls (ast_batch_set_geometry)."""
+        t = capi.BatchTune()
+        t.tpb, t.refill, t.tile = int(tpb), int(refill), int(tile)
+        check(self.lib.ast_batch_set_geometry(self.h, C.byref(t)), "ast_batch_set_geometry")
 
     def step(self, evals_per_slot: int) -> tuple:
         """One bounded launch: (done, kernel ms)."""
@@ -544,7 +552,10 @@ class Batch:
         tpb, refill, ctas = C.c_int32(0), C.c_int32(0), C.c_int32(0)
         check(self.lib.ast_batch_counters(self.h, C.byref(ne), C.byref(nf), C.byref(tpb), C.byref(refill),
                                           C.byref(ctas)), "ast_batch_counters")
-        return dict(n_evals=ne.value, n_fits=nf.value, tpb=tpb.value, refill=refill.value, ctas=ctas.value)
+        g = capi.BatchTune()
+        check(self.lib.ast_batch_geometry(self.h, C.byref(g)), "ast_batch_geometry")
+        return dict(n_evals=ne.value, n_fits=nf.value, tpb=tpb.value, refill=refill.value, ctas=ctas.value,
+                    tile=g.tile)
 
     def close(self):
         if self.h:

@@ -120,6 +120,7 @@ class BatchTune(C.Structure):
         ("refill", C.c_int32),
         ("ctas", C.c_int32),
         ("evals_per_s", C.c_double),
+        ("tile", C.c_int32),
     ]
 
 
@@ -222,6 +223,8 @@ SIGNATURES = {
     "ast_batch_counters": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int32),
                                      C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "ast_batch_destroy": (None, [_P]),
+    "ast_batch_geometry": (C.c_int, [_P, C.POINTER(BatchTune)]),
+    "ast_batch_set_geometry": (C.c_int, [_P, C.POINTER(BatchTune)]),
     "ast_server_create": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int64, C.c_int64, C.POINTER(_P)]),
     "ast_server_set_lanes": (C.c_int, [_P, C.c_int32]),
     "ast_rmsd": (C.c_int, [_P, C.POINTER(RmsdCfg), C.POINTER(RmsdOut)]),

@@ -31,6 +31,7 @@
 #include <stdio.h>
 #include <string.h>
 #include <algorithm>
+#include <type_traits>
 #include <chrono>
 #include <deque>
 #include <vector>
@@ -163,6 +164,115 @@ __global__ void __launch_bounds__(KernShape<PREC>::tpb, KernShape<PREC>::min_cta
             const BatchObj<CF>& B = objs[k];
             const ObsView o = B.L.view(B.obs, B.M.n_data);
             if (B.cancelled || slot_iterate<CF, PREC>(B.M, o, obj_view(V, B), s, R, trig, n_ev, n_fit)) {
+                atomicAdd(B.done, 1ull);
+                n_done++;
+                gchain = -1;
+                R.chain = -1;
+            }
+        }
+        if (++used >= budget) break;
+    }
+    V.chain[s] = gchain;
+    V.st[s] = R.st;
+    V.it[s] = R.l;
+    V.ev[s] = R.ev;
+    if (gchain >= 0)
+        for (int m = 0; m < objs[k].M.n_filters; m++) V.dv[(int64_t)m * S + s] = (double)R.dvl[m];
+    if (n_done) atomicAdd(&V.ctr[1], n_done);
+    if (n_ev) atomicAdd(&V.ctr[2], n_ev);
+    if (n_fit) atomicAdd(&V.ctr[3], n_fit);
+}
+
+// ---------------------------------------------------------------- warp-tiled mapping
+//
+// REFILL 32 (a warp takes 32 chains of one object at once) with the warp-tiled evaluation
+// (chi2_mixed_tile): the warp's 32 chains are evaluated together, the magnitudes of each tile of
+// T observations spread over the lanes.  Lanes whose chain is idle or whose point x2params
+// rejects take part without a result.  A warp whose chains belong to different objects, or to a
+// NUDGE object, evaluates lane by lane as batch_kernel does.  Results are those of batch_kernel
+// bit for bit.
+template <class CF, int T>
+__global__ void __launch_bounds__(KernShape<AST_PREC_MIXED>::tpb, KernShape<AST_PREC_MIXED>::min_ctas)
+    batch_tile_kernel(const BatchObj<CF>* objs, int n_objs, FitView<CF> V, int64_t budget)
+{
+    __shared__ float4 trig[kTrigTable];
+    extern __shared__ __align__(16) unsigned char tile_smem[];
+    trig_table_fill(trig);
+    __syncthreads();
+    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s >= V.n_slots) return;  // n_slots is a multiple of 32: whole warps leave
+    unsigned char* wsm = tile_smem + (size_t)(threadIdx.x >> 5) * tile_warp_bytes(T);
+    const int64_t S = V.S;
+    int64_t gchain = V.chain[s];
+    int k = 0;
+    SlotState<CF> R;
+    R.chain = -1;
+    R.st = V.st[s];
+    R.l = V.it[s];
+    R.ev = V.ev[s];
+    for (int m = 0; m < AST_MAX_FILTERS; m++) R.dvl[m] = (CF)0;
+    if (gchain >= 0) {
+        k = find_obj(objs, n_objs, gchain);
+        R.chain = gchain - objs[k].chain0;
+        for (int m = 0; m < objs[k].M.n_filters; m++) R.dvl[m] = (CF)V.dv[(int64_t)m * S + s];
+    }
+    int64_t used = 0;
+    unsigned long long n_ev = 0, n_fit = 0, n_done = 0;
+    const unsigned lane = threadIdx.x & 31u;
+    while (true) {
+        const unsigned idle = __ballot_sync(0xffffffffu, gchain < 0);
+        if (idle == 0xffffffffu) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(&V.ctr[0], 32ull);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= (unsigned long long)V.n_chains) break;
+            const unsigned long long c = base + lane;
+            if (c < (unsigned long long)V.n_chains) {
+                gchain = (int64_t)c;
+                batch_start<CF>(objs, n_objs, V, s, gchain, k, R);
+            }
+        }
+        const bool has = gchain >= 0;
+        // Cancelled objects drop their chains (counted as finished) without an evaluation.
+        const bool drop = has && objs[k].cancelled;
+        if (drop) {
+            atomicAdd(objs[k].done, 1ull);
+            n_done++;
+            gchain = -1;
+            R.chain = -1;
+        }
+        const bool live = has && !drop;
+        CF p[AST_MAX_PARAMS];
+        double params[AST_MAX_PARAMS];
+        int rej = 1;
+        if (live) {
+            const BatchObj<CF>& B = objs[k];
+            slot_point<CF>(B.M, obj_view(V, B), s, R, p);
+            rej = x2params<CF>(B.M, B.reopt, p, params);
+        } else {
+            for (int i = 0; i < AST_MAX_PARAMS; i++) params[i] = 0.5;
+        }
+        // One object for every live lane of the warp, and no NUDGE: the tiled evaluation.
+        const unsigned live_mask = __ballot_sync(0xffffffffu, live);
+        const int k0 = __shfl_sync(0xffffffffu, k, live_mask ? __ffs(live_mask) - 1 : 0);
+        const bool same = __all_sync(0xffffffffu, !live || k == k0);
+        CF fv = (CF)kHuge;
+        if (live_mask && same && !(objs[k0].M.flags & AST_NUDGE)) {
+            const BatchObj<CF>& B = objs[k0];
+            const ObsView o = B.L.view(B.obs, B.M.n_data);
+            fv = chi2_mixed_tile<CF, T>(B.M, o, params, live && !rej, R.dvl, trig, wsm);
+        } else if (live && !rej) {
+            const BatchObj<CF>& B = objs[k];
+            const ObsView o = B.L.view(B.obs, B.M.n_data);
+            fv = eval_point<CF, AST_PREC_MIXED>(B.M, o, params, R.dvl, trig);
+        }
+        if (live) {
+            const BatchObj<CF>& B = objs[k];
+            if (!rej) {
+                R.ev++;
+                n_ev++;
+            }
+            if (slot_apply<CF>(B.M, obj_view(V, B), s, R, p, rej, rej ? (CF)kHuge : fv, n_fit)) {
                 atomicAdd(B.done, 1ull);
                 n_done++;
                 gchain = -1;
@@ -534,6 +644,7 @@ struct ast_pool {
     std::vector<int> free_done;
     // launch geometry
     int tpb = 256, refill = 1, ctas = 0;
+    int tile = 0;       // warp-tiled evaluation with tiles of this many observations (0: none)
     int lanes = 1;      // lanes per chain: 1, or kCoopLanes (cooperative chains, servers only)
     size_t smem = 0;    // dynamic shared memory of the launch
     // entries
@@ -550,7 +661,7 @@ struct ast_pool {
 struct ast_batch {
     ast_pool P;
     cudaGraphExec_t graph = nullptr;
-    int g_tpb = 0, g_refill = 0, g_ctas = 0;
+    int g_tpb = 0, g_refill = 0, g_ctas = 0, g_tile = 0;
     bool ran = false;
 };
 
@@ -802,24 +913,62 @@ static int coop_geometry(ast_pool& P, int tpb)
     return AST_OK;
 }
 
-// CTA size and refill mapping -> CTAs (full occupancy, capped by the slot pool).
+// The warp-tiled kernel for tiles of T observations (double-float state; ACC pools).
+static decltype(&batch_tile_kernel<double, 16>) batch_tile_ptr(int T)
+{
+    return T == 8 ? batch_tile_kernel<double, 8> : T == 32 ? batch_tile_kernel<double, 32> : batch_tile_kernel<double, 16>;
+}
+
+// CTA size and refill mapping (and, tile > 0, the warp-tiled evaluation with tiles of that many
+// observations) -> CTAs (full occupancy, capped by the slot pool).
 template <class CF, int PREC>
-static int pool_geometry(ast_pool& P, int tpb, int refill)
+static int pool_geometry(ast_pool& P, int tpb, int refill, int tile = 0)
 {
     if (P.lanes > 1) return coop_geometry<CF, PREC>(P, 128);
     if (tpb < 32 || tpb > 256 || (tpb & 31)) return ast_set_error(AST_E_INVALID, "batch: tpb must be 32..256, x32");
     tpb = std::min(tpb, KernShape<PREC>::tpb);  // the kernel's launch bounds
     if (refill != 1 && refill != 32) return ast_set_error(AST_E_INVALID, "batch: refill must be 1 or 32");
+    if (tile && tile != 8 && tile != 16 && tile != 32)
+        return ast_set_error(AST_E_INVALID, "batch: tile must be 0, 8, 16 or 32");
+    if (tile && (PREC != AST_PREC_MIXED || !P.acc))
+        return ast_set_error(AST_E_INVALID, "batch: the warp-tiled evaluation is built for mixed-precision ACC pools");
     int occ = 0;
-    AST_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel_ptr<CF, PREC>(refill), tpb, 0));
+    size_t smem = 0;
+    if (tile) {
+        refill = 32;
+        smem = (size_t)(tpb / 32) * tile_warp_bytes(tile);
+        auto kern = batch_tile_ptr(tile);
+        if (smem > 48 * 1024) AST_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        AST_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, tpb, smem));
+    } else {
+        AST_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel_ptr<CF, PREC>(refill), tpb, 0));
+    }
     if (occ < 1) return ast_set_error(AST_E_TOO_LARGE, "batch: kernel does not fit on an SM");
     int64_t ctas = (int64_t)P.sm_count * occ;
     if (ctas * tpb > P.n_slots) ctas = P.n_slots / tpb;
     if (ctas < 1) return ast_set_error(AST_E_INVALID, "batch: slot pool smaller than one CTA");
     P.tpb = tpb;
     P.refill = refill;
+    P.tile = tile;
+    P.smem = smem;
     P.ctas = (int)ctas;
     return AST_OK;
+}
+
+// One launch of the pool's kernel (thread per chain or warp per object, or the warp-tiled
+// evaluation) on its stream.
+template <class CF, int PREC>
+static void launch_pool(ast_pool& P, const FitView<CF>& V, int64_t budget)
+{
+    if constexpr (std::is_same<CF, double>::value && PREC == AST_PREC_MIXED) {
+        if (P.tile) {  // pool_geometry allows tiles for mixed-precision ACC pools only
+            batch_tile_ptr(P.tile)<<<P.ctas, P.tpb, P.smem, P.stream>>>((const BatchObj<double>*)P.d_objs,
+                                                                       (int)P.active.size(), V, budget);
+            return;
+        }
+    }
+    batch_kernel_ptr<CF, PREC>(P.refill)<<<P.ctas, P.tpb, 0, P.stream>>>((const BatchObj<CF>*)P.d_objs,
+                                                                           (int)P.active.size(), V, budget);
 }
 
 // Per-(object, group) map of the given entries.
@@ -865,7 +1014,8 @@ template <class CF, int PREC>
 static int batch_capture(ast_batch* B)
 {
     ast_pool& P = B->P;
-    if (B->graph && B->g_tpb == P.tpb && B->g_refill == P.refill && B->g_ctas == P.ctas) return AST_OK;
+    if (B->graph && B->g_tpb == P.tpb && B->g_refill == P.refill && B->g_ctas == P.ctas && B->g_tile == P.tile)
+        return AST_OK;
     if (B->graph) { cudaGraphExecDestroy(B->graph); B->graph = nullptr; }
     std::vector<std::pair<int, Entry*>> all;
     for (size_t k = 0; k < P.active.size(); k++) all.push_back({(int)k, P.active[k]});
@@ -879,8 +1029,7 @@ static int batch_capture(ast_batch* B)
     batch_reset_kernel<<<(unsigned)((P.S + 255) / 256), 256, 0, P.stream>>>(P.chain, P.st, P.it, P.ev, P.S);
     cudaMemsetAsync(P.ctr, 0, 64, P.stream);
     cudaMemsetAsync(P.done, 0, (size_t)P.cap * 8, P.stream);
-    batch_kernel_ptr<CF, PREC>(P.refill)<<<P.ctas, P.tpb, 0, P.stream>>>((const BatchObj<CF>*)P.d_objs,
-                                                                           (int)P.active.size(), V, INT64_MAX);
+    launch_pool<CF, PREC>(P, V, INT64_MAX);
     batch_group_best_kernel<CF><<<(unsigned)n_blocks, 256, 0, P.stream>>>((const BatchObj<CF>*)P.d_objs, P.d_gmap, V);
     const cudaError_t ec = cudaStreamEndCapture(P.stream, &g);
     if (ec != cudaSuccess) return ast_set_error(AST_E_CUDA, "batch: graph capture: %s", cudaGetErrorString(ec));
@@ -890,6 +1039,7 @@ static int batch_capture(ast_batch* B)
     B->g_tpb = P.tpb;
     B->g_refill = P.refill;
     B->g_ctas = P.ctas;
+    B->g_tile = P.tile;
     return AST_OK;
 }
 
@@ -899,7 +1049,7 @@ static int batch_run_t(ast_batch* B, const ast_batch_launch* tune, double* kerne
     ast_pool& P = B->P;
     int rc;
     if (tune) {
-        if ((rc = pool_geometry<CF, PREC>(P, tune->tpb, tune->refill))) return rc;
+        if ((rc = pool_geometry<CF, PREC>(P, tune->tpb, tune->refill, tune->tile))) return rc;
     } else if (!P.ctas) {
         if ((rc = pool_geometry<CF, PREC>(P, 256, 1))) return rc;
     }
@@ -928,23 +1078,22 @@ static int batch_run_t(ast_batch* B, const ast_batch_launch* tune, double* kerne
 
 // One bounded launch from a fresh slot state: evaluations per second of this geometry.
 template <class CF, int PREC>
-static int batch_probe(ast_batch* B, int tpb, int refill, int64_t evals_per_slot, double* rate)
+static int batch_probe(ast_batch* B, int tpb, int refill, int tile, int64_t evals_per_slot, double* rate)
 {
     ast_pool& P = B->P;
-    int rc = pool_geometry<CF, PREC>(P, tpb, refill);
+    int rc = pool_geometry<CF, PREC>(P, tpb, refill, tile);
     if (rc) return rc;
     if ((rc = upload_table<CF>(P))) return rc;
     const FitView<CF> V = pool_view<CF>(P);
     batch_reset_kernel<<<(unsigned)((P.S + 255) / 256), 256, 0, P.stream>>>(P.chain, P.st, P.it, P.ev, P.S);
     AST_CUDA(cudaMemsetAsync(P.ctr, 0, 64, P.stream));
     AST_CUDA(cudaMemsetAsync(P.done, 0, (size_t)P.cap * 8, P.stream));
-    auto kern = batch_kernel_ptr<CF, PREC>(refill);
     // A first launch takes every slot through its start-up; the second is timed.
-    kern<<<P.ctas, P.tpb, 0, P.stream>>>((const BatchObj<CF>*)P.d_objs, (int)P.active.size(), V, evals_per_slot);
+    launch_pool<CF, PREC>(P, V, evals_per_slot);
     unsigned long long h0[8], h1[8];
     AST_CUDA(cudaMemcpyAsync(h0, P.ctr, sizeof(h0), cudaMemcpyDeviceToHost, P.stream));
     AST_CUDA(cudaEventRecord(P.ev0, P.stream));
-    kern<<<P.ctas, P.tpb, 0, P.stream>>>((const BatchObj<CF>*)P.d_objs, (int)P.active.size(), V, evals_per_slot);
+    launch_pool<CF, PREC>(P, V, evals_per_slot);
     AST_CUDA(cudaGetLastError());
     AST_CUDA(cudaEventRecord(P.ev1, P.stream));
     AST_CUDA(cudaMemcpyAsync(h1, P.ctr, sizeof(h1), cudaMemcpyDeviceToHost, P.stream));
@@ -960,21 +1109,35 @@ static int batch_tune_t(ast_batch* B, int64_t evals_per_slot, ast_batch_launch* 
 {
     const int tpbs[3] = {64, 128, 256};
     const int refills[2] = {1, 32};
+    const int tiles[3] = {8, 16, 32};
     double best_rate = -1;
-    ast_batch_launch bt{256, 1, 0, 0.0};
+    ast_batch_launch bt{256, 1, 0, 0.0, 0};
+    auto probe = [&](int t, int r, int tile) -> int {
+        double rate = 0;
+        int rc = batch_probe<CF, PREC>(B, t, r, tile, evals_per_slot, &rate);
+        if (rc) return rc;
+        if (rate > best_rate) {
+            best_rate = rate;
+            bt.tpb = t;
+            bt.refill = r;
+            bt.tile = tile;
+        }
+        return AST_OK;
+    };
+    // Thread per model (refill 1) and warp per object (refill 32), each lane its own chain's
+    // whole light curve; then, for mixed-precision ACC pools, the warp-tiled evaluation.
     for (int r : refills)
         for (int t : tpbs) {
             if (t > KernShape<PREC>::tpb) continue;
-            double rate = 0;
-            int rc = batch_probe<CF, PREC>(B, t, r, evals_per_slot, &rate);
-            if (rc) return rc;
-            if (rate > best_rate) {
-                best_rate = rate;
-                bt.tpb = t;
-                bt.refill = r;
-            }
+            if (int rc = probe(t, r, 0)) return rc;
         }
-    int rc = pool_geometry<CF, PREC>(B->P, bt.tpb, bt.refill);
+    if (PREC == AST_PREC_MIXED && B->P.acc)
+        for (int tile : tiles)
+            for (int t : tpbs) {
+                if (t > KernShape<PREC>::tpb) continue;
+                if (int rc = probe(t, 32, tile)) return rc;
+            }
+    int rc = pool_geometry<CF, PREC>(B->P, bt.tpb, bt.refill, bt.tile);
     if (rc) return rc;
     // Back to the untouched state: the probes ran chains that the batch will run again.
     ast_pool& P = B->P;
@@ -1000,8 +1163,7 @@ static int batch_step_t(ast_batch* B, int64_t evals_per_slot, int32_t* done, dou
     if ((rc = upload_table<CF>(P))) return rc;
     const FitView<CF> V = pool_view<CF>(P);
     AST_CUDA(cudaEventRecord(P.ev0, P.stream));
-    batch_kernel_ptr<CF, PREC>(P.refill)<<<P.ctas, P.tpb, 0, P.stream>>>((const BatchObj<CF>*)P.d_objs,
-                                                                           (int)P.active.size(), V, evals_per_slot);
+    launch_pool<CF, PREC>(P, V, evals_per_slot);
     AST_CUDA(cudaGetLastError());
     AST_CUDA(cudaEventRecord(P.ev1, P.stream));
     unsigned long long h[8];
@@ -1097,6 +1259,32 @@ extern "C" int ast_batch_result(ast_batch* B, int32_t index, ast_fit_out* out)
     const Entry* e = B->P.all[(size_t)index];
     if (e->state != 2) return ast_set_error(AST_E_INVALID, "ast_batch_result: the batch has not run");
     return copy_out(e, out);
+}
+
+template <class CF, int PREC>
+static int batch_set_geometry_t(ast_batch* B, const ast_batch_launch* g)
+{
+    return pool_geometry<CF, PREC>(B->P, g->tpb, g->refill, g->tile);
+}
+
+extern "C" int ast_batch_set_geometry(ast_batch* B, const ast_batch_launch* g)
+{
+    if (!B || !g) return ast_set_error(AST_E_INVALID, "ast_batch_set_geometry: NULL argument");
+    if (B->ran) return ast_set_error(AST_E_INVALID, "ast_batch_set_geometry: the batch has finished");
+    int rc = set_device(B->P.device);
+    if (rc) return rc;
+    return AST_DISPATCH(B->P, batch_set_geometry_t, B, g);
+}
+
+extern "C" int ast_batch_geometry(ast_batch* B, ast_batch_launch* out)
+{
+    if (!B || !out) return ast_set_error(AST_E_INVALID, "ast_batch_geometry: NULL argument");
+    out->tpb = B->P.tpb;
+    out->refill = B->P.refill;
+    out->ctas = B->P.ctas;
+    out->tile = B->P.tile;
+    out->evals_per_s = 0;
+    return AST_OK;
 }
 
 extern "C" int ast_batch_counters(ast_batch* B, int64_t* n_evals, int64_t* n_fits, int32_t* tpb, int32_t* refill,

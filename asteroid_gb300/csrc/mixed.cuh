@@ -616,6 +616,27 @@ AST_HD float mixed_vmod(const MixedFrame& F, bool bw, float phi, float theta, fl
     return ls_magnitude_f(Sp_b, Sp_c, Sp_a, Ep_b, Ep_c, Ep_a, F.ib, F.ic, F.bc);
 }
 
+// Per-filter delta_V and chi^2 from the double-float residual sums (cuda.c:887-910): the
+// combination in FP64, the sum of the filters' chi^2 over the degrees of freedom (or the RMSD).
+template <class CF>
+AST_HD CF mixed_combine(const DevModel& M, const ObsView& o, const df* sum_y, const df* sum_y2, CF* dv)
+{
+    const int N_filters = M.n_filters;
+    CF chi2m, chi2a = 0.0, SUM_w = 0.0;
+    for (int m = 0; m < N_filters; m++) {
+        const double sy = df_to_double(sum_y[m]), sy2 = df_to_double(sum_y2[m]), sw = o.sum_w[m];
+        chi2m = (CF)DD_SUB(sy2, DD_MUL(sy, sy) / sw);
+        chi2a = chi2a + chi2m;
+        dv[m] = (CF)(sy / sw);
+        SUM_w = (CF)DD_ADD((double)SUM_w, sw);
+    }
+    if (M.flags & AST_RMSD)
+        chi2a = sqrt(chi2a / SUM_w);
+    else
+        chi2a = chi2a / (CF)(M.n_data - M.n_params - N_filters);
+    return chi2a;
+}
+
 // Same contract as chi2_fp64 (model.cuh); tab is the shared-memory sin/cos table; ang_out, when
 // non-null, receives the Euler angles at every observation (reduced to [-pi, pi]).  RHS32 selects
 // the FP32 right-hand side of AST_PREC_MIXED_RHS32.
@@ -689,19 +710,8 @@ __host__ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const dou
         }
     }
     if ((flags & AST_NUDGE) && !nudge_flush(M, o, F, tab, cand, &n_cand, &Mmin, t_mod, V_mod)) return (CF)kHuge;
-    CF chi2m, chi2a = 0.0, SUM_w = 0.0;
     CF dv[AST_MAX_FILTERS];
-    for (int m = 0; m < N_filters; m++) {
-        const double sy = df_to_double(sum_y[m]), sy2 = df_to_double(sum_y2[m]), sw = o.sum_w[m];
-        chi2m = (CF)DD_SUB(sy2, DD_MUL(sy, sy) / sw);
-        chi2a = chi2a + chi2m;
-        dv[m] = (CF)(sy / sw);
-        SUM_w = (CF)DD_ADD((double)SUM_w, sw);
-    }
-    if (flags & AST_RMSD)
-        chi2a = sqrt(chi2a / SUM_w);
-    else
-        chi2a = chi2a / (CF)(N_data - M.n_params - N_filters);
+    CF chi2a = mixed_combine<CF>(M, o, sum_y, sum_y2, dv);
     if (flags & AST_NUDGE) {
         float S_M = 0.0f, P_tot = 1.0f;
         for (int imod = 0; imod < Mmin; imod++) {
@@ -744,6 +754,101 @@ __host__ __device__ CF chi2_mixed(const DevModel& M, const ObsView& o, const dou
         chi2a = chi2a * P_tot * P_M;
     }
     for (int m = 0; m < N_filters; m++) delta_V[m] = dv[m];
+    return chi2a;
+}
+
+// ---------------------------------------------------------------- warp-tiled evaluation
+//
+// Warp per model with observation tiles: the 32 lanes of a warp evaluate 32 parameter vectors of
+// one object together.  Each lane integrates its own vector through a tile of T observations and
+// leaves the Euler angles in shared memory; the warp then computes the tile's magnitudes
+// transposed -- the 32 x T (vector, observation) pairs spread over the lanes, consecutive lanes
+// on consecutive observations of one vector -- and each lane sums its own vector's residuals in
+// observation order.  The arithmetic is that of chi2_mixed, term for term, so the result is the
+// same bit for bit; what changes is which lane computes a magnitude.  The residual sums need no
+// cross-lane reduction: the transposed residuals go back to their vector's lane through shared
+// memory, which keeps the summation order, and the bits, of the thread path.  No NUDGE (its
+// minimum search runs along one vector's curve); ast_batch_tune weighs this mapping and T
+// against the thread-per-model kernels.
+
+// Shared-memory bytes of one warp: the 32 vectors' magnitude frames, their angles over a tile
+// and the tile's residuals (double-floats).
+__host__ __device__ constexpr int tile_warp_bytes(int T)
+{
+    return 4 * (kMixedFrameFloats * 32 + 3 * 32 * (T + 1)) + 8 * 32 * (T + 1);
+}
+
+__device__ __forceinline__ void frame_store(float* fr, int lane, const MixedFrame& F)
+{
+    const float* f = &F.M_x;
+#pragma unroll
+    for (int k = 0; k < kMixedFrameFloats; k++) fr[k * 32 + lane] = f[k];
+}
+
+__device__ __forceinline__ MixedFrame frame_load(const float* fr, int lane)
+{
+    MixedFrame F;
+    float* f = &F.M_x;
+#pragma unroll
+    for (int k = 0; k < kMixedFrameFloats; k++) f[k] = fr[k * 32 + lane];
+    return F;
+}
+
+// Called by all 32 lanes of a warp at once (uniform control flow), each with its own params;
+// `active` lanes get their chi^2 and delta_V, the others only take part.  wsm: the warp's
+// tile_warp_bytes(T) of shared memory.
+template <class CF, int T>
+__device__ CF chi2_mixed_tile(const DevModel& M, const ObsView& o, const double* params, bool active, CF* delta_V,
+                              const float4* tab, unsigned char* wsm)
+{
+    static_assert(sizeof(MixedFrame) == 4 * kMixedFrameFloats, "MixedFrame is kMixedFrameFloats floats");
+    const int lane = threadIdx.x & 31;
+    const int N_data = M.n_data, N_filters = M.n_filters;
+    float* fr = (float*)wsm;                          // [kMixedFrameFloats][32]
+    float* ang = fr + kMixedFrameFloats * 32;         // [3][32][T + 1]
+    float2* res = (float2*)(ang + 3 * 32 * (T + 1));  // [32][T + 1]
+    df sum_y2[AST_MAX_FILTERS], sum_y[AST_MAX_FILTERS];
+    for (int m = 0; m < N_filters; m++) { sum_y2[m] = df{0.0f, 0.0f}; sum_y[m] = df{0.0f, 0.0f}; }
+    MixedState S;
+    mixed_setup(M, params, S);
+    frame_store(fr, lane, S.F);
+    const bool bw = S.bw;
+    for (int i0 = 0; i0 < N_data; i0 += T) {
+        const int n = min(T, N_data - i0);
+        // Integrate this lane's vector through the tile.
+        for (int j = 0; j < n; j++) {
+            df a[3];
+            mixed_advance<false>(S, o, i0 + j, tab, a);
+#pragma unroll
+            for (int c = 0; c < 3; c++) ang[(c * 32 + lane) * (T + 1) + j] = DF_ADD(a[c].hi, a[c].lo);
+        }
+        __syncwarp();
+        // The tile's 32 x n magnitudes, consecutive lanes on consecutive observations.
+        for (int q = lane; q < 32 * n; q += 32) {
+            const int v = q / n, j = q - v * n, i = i0 + j;
+            const MixedFrame F = frame_load(fr, v);
+            const float Vmod = mixed_vmod(F, bw, ang[(0 * 32 + v) * (T + 1) + j], ang[(1 * 32 + v) * (T + 1) + j],
+                                          ang[(2 * 32 + v) * (T + 1) + j], o, i);
+            const df yv = two_sum(o.v[i], -Vmod);
+            res[v * (T + 1) + j] = make_float2(yv.hi, yv.lo);
+        }
+        __syncwarp();
+        // This lane's residuals in observation order (the sums of chi2_mixed).
+        for (int j = 0; j < n; j++) {
+            const int i = i0 + j;
+            const float2 r = res[lane * (T + 1) + j];
+            const df yv{r.x, r.y};
+            const int m = o.f[i];
+            const df wy = df_mul_f(yv, o.w[i]);
+            sum_y[m] = df_add_fast(sum_y[m], wy);
+            sum_y2[m] = df_add_fast(sum_y2[m], df_mul_fast(wy, yv));
+        }
+        __syncwarp();
+    }
+    CF dv[AST_MAX_FILTERS];
+    const CF chi2a = mixed_combine<CF>(M, o, sum_y, sum_y2, dv);
+    if (active)
+        for (int m = 0; m < N_filters; m++) delta_V[m] = dv[m];
     return chi2a;
 }
 

@@ -257,11 +257,13 @@ def run_batch_steps(s, precision, n_chains, group, evals_cap, budget, warmup, st
     return (e1 - e0) / (t[0] * 1e-3)
 
 
-def measure_fits(device, chains=4096, evals=2000, seed=777):
+def measure_fits(device, chains=4096, evals=2000, seed=777, precisions=("mixed",), polish_evals=300):
     """Completed fits per second, measured: config 0 (300 points, LS + TORQUE + P_PSI, FP64
     simplex) run to completion -- `chains` random-start chains of `evals` chi^2 evaluations each
-    (ast_fit, one stage, groups of 256) -- in each precision; device time of the simplex launches.
-    A fit is one chain, as in the reference (one chain per thread)."""
+    (ast_fit, one stage, groups of 256) -- in each of `precisions`; device time of the simplex
+    launches.  A fit is one chain, as in the reference (one chain per thread).  4096 chains fill
+    a fraction of the GPU, so a chain's evaluations run at their latency: the FP64 run takes
+    minutes (bench.py --mode fits), the mixed one seconds."""
     from asteroid_gb300 import api, synth
 
     with tempfile.TemporaryDirectory() as d:
@@ -272,6 +274,8 @@ def measure_fits(device, chains=4096, evals=2000, seed=777):
             eng.fit(n_chains=256, group_size=256, seed=seed, evals_cap=20)  # warm-up
             res = {}
             for prec, name in ((api.PREC_MIXED, "mixed"), (api.PREC_FP64, "fp64")):
+                if name not in precisions:
+                    continue
                 r = eng.fit(n_chains=chains, group_size=256, seed=seed, evals_cap=evals, precision=prec)
                 res[name] = r
                 sec = r.kernel_ms * 1e-3
@@ -283,8 +287,8 @@ def measure_fits(device, chains=4096, evals=2000, seed=777):
             m = res["mixed"]
             p_mixed = m.best_params[int(np.argmin(m.best_f))]
             c64, _ = eng.eval(p_mixed[None, :], api.PREC_FP64)
-            pol = eng.fit(n_chains=256, group_size=256, seed=seed + 1, evals_cap=evals, reopt=True, params0=p_mixed,
-                          precision=api.PREC_FP64)
+            pol = eng.fit(n_chains=256, group_size=256, seed=seed + 1, evals_cap=polish_evals, reopt=True,
+                          params0=p_mixed, precision=api.PREC_FP64)
             p64 = pol.best_params[0]
             dx = np.abs(api.params2x(s.model, p_mixed) - api.params2x(s.model, p64))
             out["mixed_result_vs_fp64"] = {
@@ -293,8 +297,9 @@ def measure_fits(device, chains=4096, evals=2000, seed=777):
                 "chi2_fp64_reoptimised": float(pol.best_f[0]),
                 "max_abs_dx": float(dx.max()), "dx": dx.tolist(),
                 "params_mixed": p_mixed.tolist(), "params_fp64_reoptimised": p64.tolist(),
-                "note": "parameter error of the mixed result: its best parameters against the FP64 optimum a "
-                        "256-chain FP64 re-optimisation (-reopt) finds from them, in the fit's x coordinates"}
+                "note": f"parameter error of the mixed result: its best parameters against the FP64 optimum a "
+                        f"256-chain x {polish_evals}-evaluation FP64 re-optimisation (-reopt) finds from them, in "
+                        f"the fit's x coordinates"}
     return out
 
 
@@ -357,22 +362,24 @@ def bench_compare(args, tmp, rank, world):
 
 def bench_batch(args, tmp, rank, world):
     """Config 3: uneven objects (log-uniform 50-2000 points, 1-4 filters, 3-60 day spans, LS+TORQUE
-    / BC / BW_BALL) with 1024 chains each, as one batch: the autotuned geometry, then bounded
-    timed launches (evals/s), FP64 beside it, and one graph-captured run to completion of the
-    whole batch at a small evaluation cap."""
-    import torch
-
+    / BC / BW_BALL) with 1024 chains each, as one batch: the autotuner's choice over thread per
+    model (refill 1), warp per object (refill 32) and warp per model with observation tiles (tile
+    8/16/32), then bounded timed launches (evals/s) of the tuned geometry and of each mapping,
+    FP64 beside it, and one graph-captured run to completion of the whole batch at
+    --graph-evals evaluations per chain."""
     from asteroid_gb300 import api, synth
 
     objs = synth.generate_batch(args.objects, tmp)
-    stream_events = lambda fn: (fn(), None)
     line = {"metric": METRIC, "unit": UNIT, "mode": "batch", "objects": len(objs), "chains_per_object": 1024,
             "data": "synthetic (config-3 generator)"}
-    for prec, name in ((api.PREC_MIXED, "mixed"), (api.PREC_FP64, "fp64")):
+
+    def timed_steps(prec, geometry=None):
         with api.Batch(precision=prec, acc=True) as b:
             for k, s in enumerate(objs):
                 b.add(s.model, s.obs, n_chains=1024, group_size=256, seed=17 + k, evals_cap=5000)
-            tune = b.tune(evals_per_slot=2)
+            tune = b.tune(evals_per_slot=2) if geometry is None else None
+            if geometry is not None:
+                b.set_geometry(**geometry)
             budget = 4 if prec == api.PREC_MIXED else 2
             for _ in range(args.warmup):
                 b.step(budget)
@@ -380,18 +387,32 @@ def bench_batch(args, tmp, rank, world):
             ms = 0.0
             for _ in range(args.steps):
                 ms += b.step(budget)[1]
-            e1 = b.counters()["n_evals"]
-            line[name] = {"value": (e1 - e0) / (ms * 1e-3), "tuned": tune, "timed_evals": e1 - e0, "ms": ms}
+            c = b.counters()
+            geo = {k: c[k] for k in ("tpb", "refill", "tile", "ctas")}
+            return {"value": (c["n_evals"] - e0) / (ms * 1e-3), "tuned": tune, "geometry": geo,
+                    "timed_evals": c["n_evals"] - e0, "ms": ms}
+
+    line["mixed"] = timed_steps(api.PREC_MIXED)
+    line["fp64"] = timed_steps(api.PREC_FP64)
     line["speedup_mixed_over_fp64"] = line["mixed"]["value"] / line["fp64"]["value"]
-    # The whole batch in one graph-captured persistent launch (evaluation cap 50 per chain).
+    # Each mapping of the mixed path, measured the same way.
+    line["mappings"] = {
+        "thread_per_model": timed_steps(api.PREC_MIXED, dict(tpb=128, refill=1, tile=0)),
+        "warp_per_object": timed_steps(api.PREC_MIXED, dict(tpb=128, refill=32, tile=0)),
+        "warp_per_model_tile8": timed_steps(api.PREC_MIXED, dict(tpb=64, refill=32, tile=8)),
+        "warp_per_model_tile16": timed_steps(api.PREC_MIXED, dict(tpb=64, refill=32, tile=16)),
+        "warp_per_model_tile32": timed_steps(api.PREC_MIXED, dict(tpb=64, refill=32, tile=32)),
+    }
+    # The whole batch in one graph-captured persistent launch to completion.
     with api.Batch(precision=api.PREC_MIXED, acc=True) as b:
         for k, s in enumerate(objs):
-            b.add(s.model, s.obs, n_chains=1024, group_size=256, seed=17 + k, evals_cap=50)
-        b.tune(evals_per_slot=2)
+            b.add(s.model, s.obs, n_chains=1024, group_size=256, seed=17 + k, evals_cap=args.graph_evals)
+        tune = b.tune(evals_per_slot=2)
         ms = b.run()
         c = b.counters()
-        line["graph_run"] = {"evals_cap": 50, "ms": ms, "evals": c["n_evals"], "fits": c["n_fits"],
-                             "evals_per_s": c["n_evals"] / (ms * 1e-3), "geometry": c}
+        line["graph_run"] = {"evals_cap": args.graph_evals, "ms": ms, "evals": c["n_evals"], "fits": c["n_fits"],
+                             "evals_per_s": c["n_evals"] / (ms * 1e-3), "fits_per_s": c["n_fits"] / (ms * 1e-3),
+                             "tuned": tune, "geometry": c}
     print(json.dumps(line))
 
 
@@ -833,12 +854,14 @@ def main():
     ap.add_argument("--skip-batched", action="store_true")
     ap.add_argument("--skip-fits", action="store_true", help="skip the full-length config-0 fits")
     ap.add_argument("--mode", default="fit",
-                    choices=["fit", "batch", "serve", "compare", "periodogram", "rmsd", "animate", "precisions"],
+                    choices=["fit", "batch", "serve", "compare", "periodogram", "rmsd", "animate", "precisions", "fits"],
                     help="fit: the headline line; batch: config 3 (uneven objects, one launch); "
                          "serve: config 4 (Poisson arrivals, continuous batching); compare: full fits of "
                          "--config in both precisions at one seed; periodogram: minima() of plot mode; "
                          "rmsd: RMSD confidence intervals; animate: ANIMATE frames")
     ap.add_argument("--objects", type=int, default=512, help="batch mode: objects")
+    ap.add_argument("--graph-evals", type=int, default=50,
+                    help="batch mode: evaluations per chain of the graph-captured run to completion")
     ap.add_argument("--requests", type=int, default=8, help="serve mode: requests per arrival rate")
     ap.add_argument("--lanes", type=int, default=4, choices=[1, 4], help="serve mode: lanes per chain")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -874,6 +897,9 @@ def main():
         return bench_animate(args, tmp, rank, world)
     if args.mode == "precisions":
         return bench_precisions(args, tmp, rank, world)
+    if args.mode == "fits":
+        print(json.dumps({"mode": "fits", **measure_fits(local, precisions=("mixed", "fp64"))}))
+        return
     s = make_workload(args, tmp)
     model, obs = s.model, s.obs
     eng = api.Engine(model, obs, device=local)

@@ -437,6 +437,11 @@ typedef struct ast_batch_launch {
                              object, no divergence between light curves) */
     int32_t ctas;         /* CTAs of the launch (output) */
     double evals_per_s;   /* rate measured by ast_batch_tune (output) */
+    int32_t tile;         /* 0: every lane integrates and evaluates its own chain's whole light
+                             curve; 8, 16 or 32 (refill 32, mixed-precision ACC batches): warp per
+                             model with observation tiles -- the warp's 32 chains are integrated
+                             one per lane through a tile of this many observations, then the
+                             tile's 32 x T magnitudes are spread over the lanes (same results) */
 } ast_batch_launch;
 
 /* n_slots: persistent chain slots (0 = 256 per SM). */
@@ -444,7 +449,7 @@ int ast_batch_create(int32_t device, int32_t precision, int32_t acc, int64_t n_s
 /* Upload one object; *index numbers objects from 0 in the order added. */
 int ast_batch_add(ast_batch* batch, const ast_model* model, const ast_obs_set* obs, const ast_fit_cfg* cfg,
                   int32_t* index);
-/* Autotuner: times every (tpb, refill) candidate on this batch with bounded launches of
+/* Autotuner: times every (tpb, refill, tile) candidate on this batch with bounded launches of
  * evals_per_slot evaluations per slot, keeps the fastest for ast_batch_run / ast_batch_step and
  * returns it.  Call it before those: it leaves the batch in its initial state. */
 int ast_batch_tune(ast_batch* batch, int64_t evals_per_slot, ast_batch_launch* best);
@@ -458,6 +463,11 @@ int ast_batch_step(ast_batch* batch, int64_t evals_per_slot, int32_t* done, doub
 int ast_batch_result(ast_batch* batch, int32_t index, ast_fit_out* out);
 int ast_batch_counters(ast_batch* batch, int64_t* n_evals, int64_t* n_fits, int32_t* tpb, int32_t* refill,
                        int32_t* ctas);
+/* The launch geometry the batch runs with (tpb, refill, ctas, tile); evals_per_s is 0. */
+int ast_batch_geometry(ast_batch* batch, ast_batch_launch* out);
+/* Set the geometry (tpb, refill, tile of *geometry) for the following ast_batch_step calls,
+ * instead of the tuned or default one. */
+int ast_batch_set_geometry(ast_batch* batch, const ast_batch_launch* geometry);
 void ast_batch_destroy(ast_batch* batch);
 
 /* ---------------------------------------------------------------- serving

@@ -191,3 +191,22 @@ def test_server_cancel_queued_and_running(gpu, synth_objects, lanes):
             ref = eng.fit(n_chains=cfg["n_chains"], group_size=cfg["group_size"], seed=80 + k,
                           evals_cap=cfg["evals_cap"], precision=api.PREC_MIXED)
         same(got[ids[k]], ref)
+
+
+@pytest.mark.parametrize("tile", [8, 16, 32])
+def test_warp_tiled_mapping_equals_single_fits(gpu, synth_objects, tile):
+    """Warp per model with observation tiles (ast_batch_launch.tile): the warp's 32 chains are
+    integrated one per lane through T observations, the tile's magnitudes are spread over the
+    lanes, each lane sums its own residuals.  The arithmetic is the thread path's, so every
+    object equals its single fit bit for bit; the NUDGE object (c2) takes the lane-by-lane
+    evaluation inside the same kernel."""
+    objs = [synth_objects(n) for n in OBJECTS + ["c2"]]
+    with api.Batch(precision=api.PREC_MIXED, acc=True, n_slots=152 * 32) as b:
+        for k, s in enumerate(objs):
+            b.add(s.model, s.obs, **dict(CFG, seed=90 + k))
+        b.run(tpb=64, refill=32, tile=tile)
+        c = b.counters()
+        assert c["tile"] == tile and c["refill"] == 32
+        got = [b.result(i) for i in range(len(objs))]
+    for k, s in enumerate(objs):
+        same(got[k], single(s, api.PREC_MIXED, 90 + k))
