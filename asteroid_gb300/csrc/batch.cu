@@ -899,7 +899,7 @@ static int coop_geometry(ast_pool& P, int tpb)
 {
     const size_t smem = (size_t)(tpb / kCoopLanes) * sizeof(CoopXchg<CF>);
     auto kern = coop_kernel<CF, PREC>;
-    if (smem > 48 * 1024) AST_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    AST_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int occ = 0;
     AST_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, tpb, smem));
     if (occ < 1) return ast_set_error(AST_E_TOO_LARGE, "server: cooperative kernel does not fit on an SM");
@@ -938,7 +938,9 @@ static int pool_geometry(ast_pool& P, int tpb, int refill, int tile = 0)
         refill = 32;
         smem = (size_t)(tpb / 32) * tile_warp_bytes(tile);
         auto kern = batch_tile_ptr(tile);
-        if (smem > 48 * 1024) AST_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        // Always raised to the request: without it, dynamic and static shared memory together stay
+        // within 48 KB (the sin/cos table takes 4 KB of that).
+        AST_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         AST_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, tpb, smem));
     } else {
         AST_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel_ptr<CF, PREC>(refill), tpb, 0));
