@@ -109,32 +109,37 @@ AST_HD void ode_free_df(const df* y, df* f, const df* mu, const float4* tab)
     f[2] = df_mul_fast(c1, df_sub_fast(mu[0], f[0]));
 }
 
-// One RK4 step, y <- y + h/6 K1 + h/3 K2 + h/3 K3 + h/6 K4 with K1..K4 at y, y + h/2 K1,
-// y + h/2 K2, y + h K3 (cuda.c:319-372).  hq = (h, h/2), hw = (h/6, h/3) as double-floats.
-// The four stages run through a single right-hand-side call site (a rolled loop) and the new
-// state is accumulated as the stage derivatives come, so the hot loop is one copy of the
-// right-hand side -- small enough for the instruction cache -- and only one stage derivative
-// is live at a time.  Sums and products are the integrator forms of dfloat.cuh (absolute
-// error a few u^2 of the operands).
+// One RK4 step, y <- y + h/6 (K1 + 2 K2 + 2 K3 + K4) with K1..K4 at y, y + h/2 K1, y + h/2 K2,
+// y + h K3 (cuda.c:319-372, the same combination).  hq = (h, h/2), hw = (h/6, h/3) as
+// double-floats.  The four stages run through a single right-hand-side call site (a rolled loop)
+// and the stage derivatives are summed as they come (doubling is exact), so the hot loop is one
+// copy of the right-hand side -- small enough for the instruction cache -- and only one stage
+// derivative is live at a time; the last stage needs no next-stage point.  Sums and products are
+// the integrator forms of dfloat.cuh (absolute error a few u^2 of the operands).
 template <int NODE>
 AST_HD void rk4_step_df(df* y, float4 hq, float4 hw, const df* mu, const float4* tab)
 {
-    df f[NODE], K[NODE], yn[NODE];
+    df f[NODE], K[NODE], acc[NODE];
 #pragma unroll
-    for (int j = 0; j < NODE; j++) f[j] = y[j];
+    for (int j = 0; j < NODE; j++) {
+        f[j] = y[j];
+        acc[j] = df{0.0f, 0.0f};
+    }
 #pragma unroll 1
     for (int st = 0; st < 4; st++) {
         if (NODE == 6) ode_torque_df(f, K, mu, tab); else ode_free_df(f, K, mu, tab);
-        const df c = st < 2 ? df{hq.z, hq.w} : df{hq.x, hq.y};                    // h/2, h/2, h, h
-        const df wgt = (st == 1 || st == 2) ? df{hw.z, hw.w} : df{hw.x, hw.y};   // h/6, h/3, h/3, h/6
+        const float w = (st == 1 || st == 2) ? 2.0f : 1.0f;  // K1 + 2 K2 + 2 K3 + K4
 #pragma unroll
-        for (int j = 0; j < NODE; j++) {
-            yn[j] = df_mad(st == 0 ? y[j] : yn[j], wgt, K[j]);
-            f[j] = df_mad(y[j], c, K[j]);
+        for (int j = 0; j < NODE; j++) acc[j] = df_add_fast(acc[j], df{DF_MUL(w, K[j].hi), DF_MUL(w, K[j].lo)});
+        if (st < 3) {
+            const df c = st < 2 ? df{hq.z, hq.w} : df{hq.x, hq.y};  // h/2, h/2, h
+#pragma unroll
+            for (int j = 0; j < NODE; j++) f[j] = df_mad(y[j], c, K[j]);
         }
     }
+    const df h6{hw.x, hw.y};
 #pragma unroll
-    for (int j = 0; j < NODE; j++) y[j] = yn[j];
+    for (int j = 0; j < NODE; j++) y[j] = df_mad(y[j], h6, acc[j]);
 }
 
 // ---------------------------------------------------------------- FP32 right-hand side
