@@ -48,8 +48,8 @@ UNIT = "evals/s"
 # bytes of one launch (the slot state in and out; independent of the evaluations per slot) over
 # the kernels' resident slots: 58 368 for the mixed path (three CTAs of 128 per SM), 38 912 for
 # FP64.  Other workloads scale the per-evaluation figures by their RK4 step count.
-NCU_C2 = {"rk4_steps": 12568, "mixed_fp32_flops": 3.497e7, "fp64_flops": 7.75e6,
-          "slots": 58368, "dram_bytes_mixed": 2.211e8, "dram_bytes_fp64": 5.71e6}
+NCU_C2 = {"rk4_steps": 12568, "mixed_fp32_flops": 3.37e7, "fp64_flops": 7.75e6,
+          "slots": 58368, "dram_bytes_mixed": 2.112e8, "dram_bytes_fp64": 5.71e6}
 
 
 def rk4_steps(obs, time_step):
