@@ -296,14 +296,19 @@ class Engine:
     def stream(self) -> int:
         return self.lib.ast_stream(self.ctx) or 0
 
-    def eval(self, params, precision: int = PREC_FP64):
-        """chi2one on each row of params [n, n_params] -> (chi2 [n], delta_V [n, n_filters])."""
+    def eval(self, params, precision: int = PREC_FP64, chi2_out=None, dv_out=None):
+        """chi2one on each row of params [n, n_params] -> (chi2 [n], delta_V [n, n_filters]).
+        chi2_out / dv_out: optional float64 host arrays of those shapes to write into (for
+        example views of page-locked buffers)."""
         p = np.ascontiguousarray(np.atleast_2d(params), dtype=np.float64)
         if p.shape[1] != self.n_params:
             raise ValueError(f"params must have {self.n_params} columns")
         n = p.shape[0]
-        chi2 = np.zeros(n)
-        dv = np.zeros((n, self.n_filters))
+        chi2 = np.zeros(n) if chi2_out is None else chi2_out
+        dv = np.zeros((n, self.n_filters)) if dv_out is None else dv_out
+        if chi2.shape != (n,) or dv.shape != (n, self.n_filters) or chi2.dtype != np.float64 or \
+                dv.dtype != np.float64 or not (chi2.flags.c_contiguous and dv.flags.c_contiguous):
+            raise ValueError("chi2_out / dv_out must be contiguous float64 arrays of shapes (n,), (n, n_filters)")
         check(self.lib.ast_eval_batch(self.ctx, int(precision), dptr(p), n, dptr(chi2), dptr(dv)), "ast_eval_batch")
         return chi2, dv
 

@@ -991,12 +991,17 @@ def main():
     # vectors per resident thread of the evaluation kernel (the fit's slot count), so the launch
     # fills the GPU as the fit does.
     B = 4 * slots_m
-    Pe = workload_vectors(model, B, 21 + rank, s.params_true)
+    # Page-locked host buffers for the vectors in and the results out (numpy views of pinned
+    # torch tensors), as a caller streaming batches through ast_eval_batch would keep them.
+    Pe = torch.empty((B, model.n_params), dtype=torch.float64, pin_memory=True).numpy()
+    Pe[:] = workload_vectors(model, B, 21 + rank, s.params_true)
+    ce = torch.empty(B, dtype=torch.float64, pin_memory=True).numpy()
+    de = torch.empty((B, obs.n_filters), dtype=torch.float64, pin_memory=True).numpy()
     eng.eval(Pe[:256], api.PREC_MIXED)
     t0 = time.perf_counter()
     e2e_steps = 2
     for _ in range(e2e_steps):
-        eng.eval(Pe, api.PREC_MIXED)
+        eng.eval(Pe, api.PREC_MIXED, chi2_out=ce, dv_out=de)
     e2e_dt = max_over_ranks(dist, time.perf_counter() - t0)
     e2e = sum_over_ranks(dist, B * e2e_steps) / e2e_dt
 
@@ -1064,7 +1069,8 @@ def main():
                                        "per_eval_fp64_flops_executed": NCU_C2["fp64_flops"] * scale}},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": B * model.n_params * 8,
-                    "d2h_bytes_per_step": B * (1 + obs.n_filters) * 8, "path": "ast_eval_batch, mixed, host buffers"},
+                    "d2h_bytes_per_step": B * (1 + obs.n_filters) * 8,
+                    "path": "ast_eval_batch, mixed, page-locked host buffers, copies inside the timed region"},
             "gpu_launches": launches_m,
             "clocks": clocks,
         }
