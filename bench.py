@@ -776,7 +776,7 @@ def bench_serve(args, tmp, rank, world):
     engines = {}
     # The latency floor: one request alone on the GPU, for each of the first four pool objects.
     alone = []
-    for k in range(4):
+    for k in range(args.alone):
         s = pool[k]
         with api.Server(precision=api.PREC_MIXED, acc=True, hbm_budget=150 << 30, lanes=args.lanes) as srv:
             r = srv.submit(s.model, s.obs, n_chains=1024, group_size=256, seed=100 + k, evals_cap=5000,
@@ -786,7 +786,8 @@ def bench_serve(args, tmp, rank, world):
             alone.append({"n_data": s.obs.n_data, "span_days": float(s.obs.mjd[-1] - s.obs.mjd[0]),
                           "model": api.flag_names(s.model.flags), "latency_s": srv.poll(r)[1]})
     line["alone"] = alone
-    for lam in (1.0, 4.0, 16.0, 64.0):
+    print(json.dumps({"mode": "serve", "alone": alone, "lanes_per_chain": args.lanes}), flush=True)
+    for lam in [float(r) for r in args.rates.split(",")]:
         arrivals = np.cumsum(rng.exponential(1.0 / lam, size=args.requests))
         with api.Server(precision=api.PREC_MIXED, acc=True, hbm_budget=150 << 30, lanes=args.lanes) as srv:
             t0 = time.perf_counter()
@@ -831,6 +832,9 @@ def bench_serve(args, tmp, rank, world):
         line["rates"][f"{lam:g}/s"] = {"p50_s": float(np.percentile(L, 50)), "p99_s": float(np.percentile(L, 99)),
                                        "fits_per_s": len(ids) / wall, "wall_s": wall,
                                        "evals_per_s": st["n_evals"] / (st["kernel_ms"] * 1e-3)}
+        # One line per rate as it completes (a long run keeps what it measured).
+        print(json.dumps({"mode": "serve", "rate": f"{lam:g}/s", **line["rates"][f"{lam:g}/s"],
+                          "requests": args.requests, "lanes_per_chain": args.lanes}), flush=True)
     for e in engines.values():
         e.close()
     good = [rel for rel, cond in checked if cond <= 1e-10]
@@ -869,6 +873,8 @@ def main():
                     help="batch mode: evaluations per chain of the graph-captured run to completion")
     ap.add_argument("--requests", type=int, default=8, help="serve mode: requests per arrival rate")
     ap.add_argument("--lanes", type=int, default=4, choices=[1, 4], help="serve mode: lanes per chain")
+    ap.add_argument("--alone", type=int, default=4, help="serve mode: requests timed alone (the latency floor)")
+    ap.add_argument("--rates", default="1,4,16,64", help="serve mode: arrival rates, requests/s")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--profile", action="store_true", help="only the fit launches (for ncu)")
