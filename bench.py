@@ -397,6 +397,11 @@ def bench_batch(args, tmp, rank, world):
             return {"value": (c["n_evals"] - e0) / (ms * 1e-3), "tuned": tune, "geometry": geo,
                     "timed_evals": c["n_evals"] - e0, "ms": ms}
 
+    if args.profile:
+        # Only the warp-tiled kernel on this batch (the command profiled under ncu).
+        print(json.dumps({"profile": "batch_tile_kernel",
+                          **timed_steps(api.PREC_MIXED, dict(tpb=64, refill=32, tile=16))}))
+        return
     line["mixed"] = timed_steps(api.PREC_MIXED)
     line["fp64"] = timed_steps(api.PREC_FP64)
     line["speedup_mixed_over_fp64"] = line["mixed"]["value"] / line["fp64"]["value"]
