@@ -76,7 +76,7 @@ def test_fp64_matches_reference_kernel_on_fixtures(gpu, oracle_mod, path):
     # 50 x cond (by up to 3e-11 on 256-400 vectors per variant); none comes near 1e-10.
     within = rel <= bound
     assert rel.size > 0 and np.mean(within) >= 0.95 and rel.max() <= 1e-10, f"max rel {rel.max():.3e}"
-    assert np.mean(rel <= RTOL) >= 0.8
+    assert np.mean(rel <= RTOL) >= 0.82  # measured 0.85-1.00 per variant (0.84 at the lowest in an earlier run)
     dv_ok = np.abs(dv - ref_dv) <= np.maximum(1e-12, bound[:, None] * 10) * np.maximum(np.abs(ref_dv), 1)
     assert np.all(dv_ok[within])
 
@@ -95,7 +95,7 @@ def test_fp64_matches_reference_kernel_on_configs(gpu, oracle_mod, synth_objects
     rel, nfin, *_, bound = _compare(m, s.obs, np.array(P), variant, oracle_mod)
     assert not nfin.any()
     assert np.mean(rel <= bound) >= 0.95 and rel.max() <= 1e-10, f"max rel {rel.max():.3e}"
-    assert np.mean(rel <= RTOL) >= 0.8
+    assert np.mean(rel <= RTOL) >= 0.82  # measured 0.85-1.00 per variant (0.84 at the lowest in an earlier run)
 
 
 def test_throughput_against_the_reference_kernel_on_c2(gpu, oracle_mod, synth_objects):
