@@ -601,6 +601,7 @@ struct Entry {
     int done_slot = -1;
     std::vector<double> res_f, res_p, res_dv;
     double t_submit = 0, t_admit = 0, t_done = 0;
+    double cost = 0;  // RK4 steps plus observations of one evaluation (ordering of a batch)
 };
 
 size_t entry_bytes(Entry& e, int cfb)
@@ -662,6 +663,7 @@ struct ast_batch {
     ast_pool P;
     cudaGraphExec_t graph = nullptr;
     int g_tpb = 0, g_refill = 0, g_ctas = 0, g_tile = 0;
+    bool ordered = false;
     bool ran = false;
 };
 
@@ -786,6 +788,11 @@ static int pool_new_entry(ast_pool& P, const ast_model* model, const ast_obs_set
             for (int i = 0; i < e->N; i++) e->x_start[g * e->N + i] = x[i];
     }
     e->bytes = entry_bytes(*e, P.cfb);
+    // Work of one evaluation: the RK4 steps between consecutive observations (cuda.c:321) and a
+    // magnitude per observation.
+    e->cost = (double)obs->n_data;
+    for (int i = 1; i < obs->n_data; i++)
+        e->cost += (double)(int)((obs->mjd[i] - obs->mjd[i - 1]) / model->time_step) + 1.0;
     e->id = (int64_t)P.all.size();
     e->t_submit = now_s();
     P.all.push_back(e);
@@ -1012,6 +1019,24 @@ static int copy_out(const Entry* e, ast_fit_out* out)
 
 // ---------------------------------------------------------------- batch
 
+// Before a batch's first launch: its objects take the chain index space longest evaluation
+// first, so the chains that run longest start first and the launch does not end on a tail of a
+// few long chains (longest-processing-time-first order).  A chain's index within its object --
+// its random draws and its result -- does not change.
+static void batch_order(ast_batch* B)
+{
+    if (B->ordered) return;
+    ast_pool& P = B->P;
+    std::stable_sort(P.active.begin(), P.active.end(), [](const Entry* a, const Entry* b) { return a->cost > b->cost; });
+    int64_t c = 0;
+    for (Entry* e : P.active) {
+        e->chain0 = c;
+        c += e->n_chains;
+    }
+    P.table_dirty = true;
+    B->ordered = true;
+}
+
 template <class CF, int PREC>
 static int batch_capture(ast_batch* B)
 {
@@ -1049,6 +1074,7 @@ template <class CF, int PREC>
 static int batch_run_t(ast_batch* B, const ast_batch_launch* tune, double* kernel_ms)
 {
     ast_pool& P = B->P;
+    batch_order(B);
     int rc;
     if (tune) {
         if ((rc = pool_geometry<CF, PREC>(P, tune->tpb, tune->refill, tune->tile))) return rc;
@@ -1109,6 +1135,7 @@ static int batch_probe(ast_batch* B, int tpb, int refill, int tile, int64_t eval
 template <class CF, int PREC>
 static int batch_tune_t(ast_batch* B, int64_t evals_per_slot, ast_batch_launch* best)
 {
+    batch_order(B);
     const int tpbs[3] = {64, 128, 256};
     const int refills[2] = {1, 32};
     const int tiles[3] = {8, 16, 32};
@@ -1160,6 +1187,7 @@ template <class CF, int PREC>
 static int batch_step_t(ast_batch* B, int64_t evals_per_slot, int32_t* done, double* kernel_ms)
 {
     ast_pool& P = B->P;
+    batch_order(B);
     int rc;
     if (!P.ctas && (rc = pool_geometry<CF, PREC>(P, 256, 1))) return rc;
     if ((rc = upload_table<CF>(P))) return rc;
