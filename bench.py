@@ -402,11 +402,12 @@ def bench_batch(args, tmp, rank, world):
         print(json.dumps({"profile": "batch_tile_kernel",
                           **timed_steps(api.PREC_MIXED, dict(tpb=64, refill=32, tile=16))}))
         return
-    line["mixed"] = timed_steps(api.PREC_MIXED)
-    line["fp64"] = timed_steps(api.PREC_FP64)
-    line["speedup_mixed_over_fp64"] = line["mixed"]["value"] / line["fp64"]["value"]
+    if not args.graph_only:
+        line["mixed"] = timed_steps(api.PREC_MIXED)
+        line["fp64"] = timed_steps(api.PREC_FP64)
+        line["speedup_mixed_over_fp64"] = line["mixed"]["value"] / line["fp64"]["value"]
     # Each mapping of the mixed path, measured the same way.
-    line["mappings"] = {
+    line["mappings"] = {} if args.graph_only else {
         "thread_per_model": timed_steps(api.PREC_MIXED, dict(tpb=128, refill=1, tile=0)),
         "warp_per_object": timed_steps(api.PREC_MIXED, dict(tpb=128, refill=32, tile=0)),
         "warp_per_model_tile8": timed_steps(api.PREC_MIXED, dict(tpb=64, refill=32, tile=8)),
@@ -874,6 +875,7 @@ def main():
                          "--config in both precisions at one seed; periodogram: minima() of plot mode; "
                          "rmsd: RMSD confidence intervals; animate: ANIMATE frames")
     ap.add_argument("--objects", type=int, default=512, help="batch mode: objects")
+    ap.add_argument("--graph-only", action="store_true", help="batch mode: only the graph-captured run")
     ap.add_argument("--graph-evals", type=int, default=50,
                     help="batch mode: evaluations per chain of the graph-captured run to completion")
     ap.add_argument("--requests", type=int, default=8, help="serve mode: requests per arrival rate")
