@@ -294,6 +294,132 @@ AST_HD void df_sincos(df a, const float4* __restrict__ table, df* s_out, df* c_o
     *c_out = df_sub_fast(df_mul_fast(C, ce), df_mul_fast(S, sig));
 }
 
+// ------------------------------------------------ packed pairs
+//
+// df2 holds two double-floats side by side, (hi.x + lo.x) and (hi.y + lo.y).  Each operation
+// below is its scalar namesake applied to both lanes, with the same roundings in the same order,
+// so a lane's result is bit for bit the scalar one.  On the device a pair is one packed FP32x2
+// instruction (add/mul/fma .rn.f32x2 of sm_100 and later, the __fadd2_rn family): one issue slot
+// for two lanes of arithmetic, where the FP32 pipe itself processes the same number of lanes
+// either way.  A negated operand folds into the packed instruction.  Every packed product below
+// either is exact or has a second use, except the sincos table index, which is scalar (see
+// df2_sincos).  On the host the lanes are computed one after the other.
+struct df2 {
+    float2 hi, lo;
+};
+
+AST_HD float2 f2(float a) { return make_float2(a, a); }
+AST_HD float2 f2_neg(float2 a) { return make_float2(-a.x, -a.y); }
+AST_HD float2 f2_add(float2 a, float2 b)
+{
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+    return __fadd2_rn(a, b);
+#else
+    return make_float2(DF_ADD(a.x, b.x), DF_ADD(a.y, b.y));
+#endif
+}
+AST_HD float2 f2_sub(float2 a, float2 b) { return f2_add(a, f2_neg(b)); }
+AST_HD float2 f2_mul(float2 a, float2 b)
+{
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+    return __fmul2_rn(a, b);
+#else
+    return make_float2(DF_MUL(a.x, b.x), DF_MUL(a.y, b.y));
+#endif
+}
+AST_HD float2 f2_fma(float2 a, float2 b, float2 c)
+{
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+    return __ffma2_rn(a, b, c);
+#else
+    return make_float2(DF_FMA(a.x, b.x, c.x), DF_FMA(a.y, b.y, c.y));
+#endif
+}
+
+AST_HD df2 df2_pack(df a, df b) { return df2{make_float2(a.hi, b.hi), make_float2(a.lo, b.lo)}; }
+AST_HD df df2_x(df2 a) { return df{a.hi.x, a.lo.x}; }
+AST_HD df df2_y(df2 a) { return df{a.hi.y, a.lo.y}; }
+AST_HD df2 df2_neg(df2 a) { return df2{f2_neg(a.hi), f2_neg(a.lo)}; }
+
+AST_HD df2 two_sum2(float2 a, float2 b)
+{
+    const float2 s = f2_add(a, b);
+    const float2 bb = f2_sub(s, a);
+    return df2{s, f2_add(f2_sub(a, f2_sub(s, bb)), f2_sub(b, bb))};
+}
+AST_HD df2 fast_two_sum2(float2 a, float2 b)
+{
+    const float2 s = f2_add(a, b);
+    return df2{s, f2_sub(b, f2_sub(s, a))};
+}
+AST_HD df2 two_prod2(float2 a, float2 b)
+{
+    const float2 p = f2_mul(a, b);
+    return df2{p, f2_fma(a, b, f2_neg(p))};
+}
+AST_HD df2 df2_add_fast(df2 x, df2 y)
+{
+    const df2 s = two_sum2(x.hi, y.hi);
+    return fast_two_sum2(s.hi, f2_add(x.lo, f2_add(y.lo, s.lo)));
+}
+AST_HD df2 df2_sub_fast(df2 x, df2 y) { return df2_add_fast(x, df2_neg(y)); }
+AST_HD df2 df2_add_f(df2 x, float2 y)
+{
+    const df2 s = two_sum2(x.hi, y);
+    return fast_two_sum2(s.hi, f2_add(x.lo, s.lo));
+}
+AST_HD df2 df2_mul_fast(df2 x, df2 y)
+{
+    const df2 c = two_prod2(x.hi, y.hi);
+    return fast_two_sum2(c.hi, f2_fma(x.lo, y.hi, f2_fma(x.hi, y.lo, c.lo)));
+}
+AST_HD df2 df2_mad(df2 y, df2 c, df2 k)
+{
+    const float2 p = f2_mul(c.hi, k.hi);
+    const float2 pe = f2_fma(c.lo, k.hi, f2_fma(c.hi, k.lo, f2_fma(c.hi, k.hi, f2_neg(p))));
+    const df2 s = two_sum2(y.hi, p);
+    return fast_two_sum2(s.hi, f2_add(f2_add(y.lo, pe), s.lo));
+}
+
+// sin and cos of two double-float angles at once: df_sincos lane by lane.
+AST_HD void df2_sincos(df2 a, const float4* __restrict__ table, df2* s_out, df2* c_out)
+{
+    if (fabsf(a.hi.x) > 65536.0f || fabsf(a.hi.y) > 65536.0f) {
+        const df ax = fabsf(a.hi.x) > 65536.0f ? df_reduce_2pi(df2_x(a)) : df2_x(a);
+        const df ay = fabsf(a.hi.y) > 65536.0f ? df_reduce_2pi(df2_y(a)) : df2_y(a);
+        a = df2_pack(ax, ay);
+    }
+    const float inv_step = (float)(kTrigTable / (2.0 * 3.14159265358979323846));
+    const float magic = 12582912.0f;
+    // The table index in scalar operations: the compiler contracts a packed product whose only use
+    // is a packed add into one fused multiply-add, even written as mul.rn.f32x2 and add.rn.f32x2
+    // (measured on sm_103a), and the fused round(a*c + m) picks the neighbouring table point
+    // where a*c lies within its rounding error of a half-integer.  Scalar .rn operations are
+    // never merged, so k is the scalar df_sincos's.
+    const float2 kb = make_float2(DF_ADD(DF_MUL(a.hi.x, inv_step), magic), DF_ADD(DF_MUL(a.hi.y, inv_step), magic));
+    const float2 k = f2_sub(kb, f2(magic));
+    const float4 T0 = table[DF_BITS(kb.x) & (kTrigTable - 1)];
+    const float4 T1 = table[DF_BITS(kb.y) & (kTrigTable - 1)];
+    const float2 e0 = f2_fma(f2_neg(k), f2(0.02454369328916073f), a.hi);
+    df2 e = two_sum2(e0, a.lo);
+    e = df2_sub_fast(e, two_prod2(k, f2(-6.829904419802801e-10f)));
+    e = df2_add_f(e, f2_neg(f2_mul(k, f2(-2.6798820468841904e-17f))));
+    const float2 e1 = e.hi;
+    const float2 e2 = f2_mul(e1, e1);
+    const float2 q = f2_mul(f2_mul(e2, f2(1.0f / 6.0f)),
+                            f2_fma(e2, f2_fma(e2, f2(1.0f / 840.0f), f2(-1.0f / 20.0f)), f2(1.0f)));
+    const df2 sig = df2_add_f(e, f2_neg(f2_fma(f2_mul(f2(0.5f), e2), e.lo, f2_mul(e1, q))));
+    const float2 h2l = f2_fma(f2_mul(f2(2.0f), e1), e.lo, f2_fma(e1, e1, f2_neg(e2)));
+    const float2 e4 = f2_mul(e2, e2);
+    const float2 tail = f2_mul(f2_mul(e4, f2(1.0f / 24.0f)), f2_fma(e2, f2(-1.0f / 30.0f), f2(1.0f)));
+    const df2 c0 = fast_two_sum2(f2(1.0f), f2_mul(f2(-0.5f), e2));
+    const df2 ce = fast_two_sum2(c0.hi, f2_add(c0.lo, f2_fma(f2(-0.5f), h2l, tail)));
+    const df2 S{make_float2(T0.x, T1.x), make_float2(T0.y, T1.y)};
+    const df2 C{make_float2(T0.z, T1.z), make_float2(T0.w, T1.w)};
+    *s_out = df2_add_fast(df2_mul_fast(S, ce), df2_mul_fast(C, sig));
+    *c_out = df2_sub_fast(df2_mul_fast(C, ce), df2_mul_fast(S, sig));
+}
+
 // ------------------------------------------------ sqrt, atan2, log
 
 // sqrt(x), x >= 0: the FP32 root corrected once with the double-float residual.

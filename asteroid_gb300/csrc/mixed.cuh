@@ -69,77 +69,74 @@ AST_HD float ls_magnitude_f(float Sb, float Sc, float Sa, float Eb, float Ec, fl
     return DF_MUL(-2.5f, log10f(DF_MUL(DF_MUL(DF_MUL(bc, sS), sE) / scalar, B)));
 }
 
-// sin and cos of two double-float angles through one copy of df_sincos (a rolled loop keeps
-// the right-hand side small enough for the instruction cache).
-AST_HD void df_sincos2(df a0, df a1, const float4* tab, df* s0, df* c0, df* s1, df* c1)
+// The rotation ODEs (cuda.c:13-77) in double-float, on the state in packed pairs (df2): the
+// sin and cos of the two angles the right-hand side needs are one df2_sincos, its products and
+// quotient are the scalar double-float operations on the pairs' halves.  Pair layout, torque:
+// (y0, y1), (y2, phi), (psi, theta), where y0..y2 are the body-frame angular velocities of
+// cuda.c:46-58; free rotation (cuda.c:69-75): (psi, theta), (phi, unused 0).  mu: torque
+// ((Is-1)/Ii, (1-Ii)/Is, Ii-Is, Ti, Ts, Tl); free (L, Ip, Im).
+AST_HD void ode_torque_df2(const df2* y, df2* f, const df* mu, const float4* tab)
 {
-#pragma unroll 1
-    for (int q = 0; q < 2; q++) {
-        df s, c;
-        df_sincos(q ? a1 : a0, tab, &s, &c);
-        // Selects, not an array indexed by q: the results stay in registers.
-        if (q == 0) {
-            *s0 = s;
-            *c0 = c;
-        } else {
-            *s1 = s;
-            *c1 = c;
-        }
-    }
+    df2 s, c;
+    df2_sincos(y[2], tab, &s, &c);  // (sin psi, sin theta), (cos psi, cos theta)
+    const df y0 = df2_x(y[0]), y1 = df2_y(y[0]), y2 = df2_x(y[1]);
+    const df s5 = df2_x(s), s4 = df2_y(s), c5 = df2_x(c), c4 = df2_y(c);
+    const df f0 = df_add_fast(df_mul_fast(df_mul_fast(mu[0], y1), y2), mu[3]);
+    const df f1 = df_add_fast(df_mul_fast(df_mul_fast(mu[1], y2), y0), mu[4]);
+    const df f2 = df_add_fast(df_mul_fast(df_mul_fast(mu[2], y0), y1), mu[5]);
+    const df f3 = df_div_fast(df_add_fast(df_mul_fast(y0, s5), df_mul_fast(y1, c5)), s4);
+    const df f4 = df_sub_fast(df_mul_fast(y0, c5), df_mul_fast(y1, s5));
+    const df f5 = df_sub_fast(y2, df_mul_fast(f3, c4));
+    f[0] = df2_pack(f0, f1);
+    f[1] = df2_pack(f2, f3);
+    f[2] = df2_pack(f5, f4);
 }
 
-AST_HD void ode_torque_df(const df* y, df* f, const df* mu, const float4* tab)
+AST_HD void ode_free_df2(const df2* y, df2* f, const df* mu, const float4* tab)
 {
-    df s5, c5, s4, c4;
-    df_sincos2(y[5], y[4], tab, &s5, &c5, &s4, &c4);
-    f[0] = df_add_fast(df_mul_fast(df_mul_fast(mu[0], y[1]), y[2]), mu[3]);
-    f[1] = df_add_fast(df_mul_fast(df_mul_fast(mu[1], y[2]), y[0]), mu[4]);
-    f[2] = df_add_fast(df_mul_fast(df_mul_fast(mu[2], y[0]), y[1]), mu[5]);
-    f[3] = df_div_fast(df_add_fast(df_mul_fast(y[0], s5), df_mul_fast(y[1], c5)), s4);
-    f[4] = df_sub_fast(df_mul_fast(y[0], c5), df_mul_fast(y[1], s5));
-    f[5] = df_sub_fast(y[2], df_mul_fast(f[3], c4));
-}
-
-AST_HD void ode_free_df(const df* y, df* f, const df* mu, const float4* tab)
-{
-    df s2, c2, s1, c1;
-    df_sincos2(df{2.0f * y[2].hi, 2.0f * y[2].lo}, y[1], tab, &s2, &c2, &s1, &c1);
-    f[0] = df_mul_fast(mu[0], df_sub_fast(mu[1], df_mul_fast(mu[2], c2)));
-    f[1] = df_mul_fast(df_mul_fast(df_mul_fast(mu[0], mu[2]), s1), s2);
-    f[2] = df_mul_fast(c1, df_sub_fast(mu[0], f[0]));
+    df2 s, c;  // of (2 psi, theta): doubling is exact
+    df2_sincos(df2{f2_mul(y[0].hi, make_float2(2.0f, 1.0f)), f2_mul(y[0].lo, make_float2(2.0f, 1.0f))}, tab, &s, &c);
+    const df s2 = df2_x(s), c2 = df2_x(c), s1 = df2_y(s), c1 = df2_y(c);
+    const df dphi = df_mul_fast(mu[0], df_sub_fast(mu[1], df_mul_fast(mu[2], c2)));
+    const df dtheta = df_mul_fast(df_mul_fast(df_mul_fast(mu[0], mu[2]), s1), s2);
+    const df dpsi = df_mul_fast(c1, df_sub_fast(mu[0], dphi));
+    f[0] = df2_pack(dpsi, dtheta);
+    f[1] = df2_pack(dphi, df{0.0f, 0.0f});
 }
 
 // One RK4 step, y <- y + h/6 (K1 + 2 K2 + 2 K3 + K4) with K1..K4 at y, y + h/2 K1, y + h/2 K2,
-// y + h K3 (cuda.c:319-372, the same combination).  hq = (h, h/2), hw = (h/6, h/3) as
-// double-floats.  The four stages run through a single right-hand-side call site (a rolled loop)
-// and the stage derivatives are summed as they come (doubling is exact), so the hot loop is one
-// copy of the right-hand side -- small enough for the instruction cache -- and only one stage
-// derivative is live at a time; the last stage needs no next-stage point.  Sums and products are
-// the integrator forms of dfloat.cuh (absolute error a few u^2 of the operands).
+// y + h K3 (cuda.c:319-372, the same combination), on the packed pairs of the ODE's layout
+// (NODE = 6 torque, 3 free).  hq = (h, h/2), hw = (h/6, h/3) as double-floats.  The four stages
+// run through a single right-hand-side call site (a rolled loop) and the stage derivatives are
+// summed as they come (doubling is exact), so the hot loop is one copy of the right-hand side --
+// small enough for the instruction cache -- and only one stage derivative is live at a time; the
+// last stage needs no next-stage point.  Sums and products are the integrator forms of
+// dfloat.cuh (absolute error a few u^2 of the operands), two components per instruction.
 template <int NODE>
-AST_HD void rk4_step_df(df* y, float4 hq, float4 hw, const df* mu, const float4* tab)
+AST_HD void rk4_step_df2(df2* y, float4 hq, float4 hw, const df* mu, const float4* tab)
 {
-    df f[NODE], K[NODE], acc[NODE];
+    constexpr int P = (NODE + 1) / 2;
+    df2 f[P], K[P], acc[P];
 #pragma unroll
-    for (int j = 0; j < NODE; j++) {
+    for (int j = 0; j < P; j++) {
         f[j] = y[j];
-        acc[j] = df{0.0f, 0.0f};
+        acc[j] = df2{f2(0.0f), f2(0.0f)};
     }
 #pragma unroll 1
     for (int st = 0; st < 4; st++) {
-        if (NODE == 6) ode_torque_df(f, K, mu, tab); else ode_free_df(f, K, mu, tab);
-        const float w = (st == 1 || st == 2) ? 2.0f : 1.0f;  // K1 + 2 K2 + 2 K3 + K4
+        if (NODE == 6) ode_torque_df2(f, K, mu, tab); else ode_free_df2(f, K, mu, tab);
+        const float2 w = f2((st == 1 || st == 2) ? 2.0f : 1.0f);  // K1 + 2 K2 + 2 K3 + K4
 #pragma unroll
-        for (int j = 0; j < NODE; j++) acc[j] = df_add_fast(acc[j], df{DF_MUL(w, K[j].hi), DF_MUL(w, K[j].lo)});
+        for (int j = 0; j < P; j++) acc[j] = df2_add_fast(acc[j], df2{f2_mul(w, K[j].hi), f2_mul(w, K[j].lo)});
         if (st < 3) {
-            const df c = st < 2 ? df{hq.z, hq.w} : df{hq.x, hq.y};  // h/2, h/2, h
+            const df2 c = st < 2 ? df2{f2(hq.z), f2(hq.w)} : df2{f2(hq.x), f2(hq.y)};  // h/2, h/2, h
 #pragma unroll
-            for (int j = 0; j < NODE; j++) f[j] = df_mad(y[j], c, K[j]);
+            for (int j = 0; j < P; j++) f[j] = df2_mad(y[j], c, K[j]);
         }
     }
-    const df h6{hw.x, hw.y};
+    const df2 h6{f2(hw.x), f2(hw.y)};
 #pragma unroll
-    for (int j = 0; j < NODE; j++) y[j] = df_mad(y[j], h6, acc[j]);
+    for (int j = 0; j < P; j++) y[j] = df2_mad(y[j], h6, acc[j]);
 }
 
 // ---------------------------------------------------------------- FP32 right-hand side
@@ -168,7 +165,7 @@ AST_HD void f_sincos_tab(float a, const float4* __restrict__ tab, float* s, floa
     *c = DF_FMA(-T.x, se, DF_FMA(-T.z, hc, T.z)); // C cos e - S sin e
 }
 
-// cuda.c:46-58 in FP32.  mu as in ode_torque_df.
+// cuda.c:46-58 in FP32.  mu as in ode_torque_df2.
 AST_HD void ode_torque_f32(const float* y, float* f, const float* mu, const float4* tab)
 {
     float s5, c5, s4, c4;
@@ -544,11 +541,22 @@ AST_HD void mixed_advance(MixedState& S, const ObsView& o, int i, const float4* 
                 for (int l = 0; l < N_steps; l++) rk4_step_f32<3>(S.y, hq, hw, S.muf, tab);
             }
         } else if (S.torque) {
+            df2 Y[3] = {df2_pack(S.y[0], S.y[1]), df2_pack(S.y[2], S.y[3]), df2_pack(S.y[5], S.y[4])};
 #pragma unroll 1
-            for (int l = 0; l < N_steps; l++) rk4_step_df<6>(S.y, hq, hw, S.mu, tab);
+            for (int l = 0; l < N_steps; l++) rk4_step_df2<6>(Y, hq, hw, S.mu, tab);
+            S.y[0] = df2_x(Y[0]);
+            S.y[1] = df2_y(Y[0]);
+            S.y[2] = df2_x(Y[1]);
+            S.y[3] = df2_y(Y[1]);
+            S.y[5] = df2_x(Y[2]);
+            S.y[4] = df2_y(Y[2]);
         } else {
+            df2 Y[2] = {df2_pack(S.y[2], S.y[1]), df2_pack(S.y[0], df{0.0f, 0.0f})};
 #pragma unroll 1
-            for (int l = 0; l < N_steps; l++) rk4_step_df<3>(S.y, hq, hw, S.mu, tab);
+            for (int l = 0; l < N_steps; l++) rk4_step_df2<3>(Y, hq, hw, S.mu, tab);
+            S.y[2] = df2_x(Y[0]);
+            S.y[1] = df2_y(Y[0]);
+            S.y[0] = df2_x(Y[1]);
         }
     }
     // (Constant indices only: an index computed at run time would move y to local memory.)
