@@ -43,13 +43,15 @@ UNIT = "evals/s"
 # Executed work per evaluation on the config-2 workload, from ncu captures of the two fit
 # kernels (sm__sass_thread_inst_executed_op_{ffma,fadd,fmul}_pred_on.sum and the d* FP64
 # counterparts, dram__bytes_read.sum + dram__bytes_write.sum): FP32 flops of the mixed path
-# (FFMA x 2 + FADD + FMUL, the double-float formulation's own arithmetic), FP64 flops of the
-# plain path (DFMA x 2 + DADD + DMUL, including the FP64 transcendental functions), and DRAM
-# bytes of one launch (the slot state in and out; independent of the evaluations per slot) over
-# the kernels' resident slots: 58 368 for the mixed path (three CTAs of 128 per SM), 38 912 for
+# (FFMA x 2 + FADD + FMUL, the double-float formulation's own arithmetic; counted on the scalar
+# build of the step -- the packed FP32x2 build performs the same lane operations, bit for bit,
+# in fewer instructions, and those counters see only its scalar part), FP64 flops of the plain
+# path (DFMA x 2 + DADD + DMUL, including the FP64 transcendental functions), and DRAM bytes of
+# one launch (the slot state in and out; independent of the evaluations per slot) over the
+# kernels' resident slots: 58 368 for the mixed path (three CTAs of 128 per SM), 38 912 for
 # FP64.  Other workloads scale the per-evaluation figures by their RK4 step count.
 NCU_C2 = {"rk4_steps": 12568, "mixed_fp32_flops": 3.37e7, "fp64_flops": 7.75e6,
-          "slots": 58368, "dram_bytes_mixed": 2.112e8, "dram_bytes_fp64": 5.71e6}
+          "slots": 58368, "dram_bytes_mixed": 1.619e8, "dram_bytes_fp64": 5.71e6}
 
 
 def rk4_steps(obs, time_step):
