@@ -7,10 +7,13 @@ moves chi^2, are reported but not held to it.  Under NUDGE the count of model mi
 discontinuous function of the model magnitudes, so a near-tie decided differently in FP32
 changes the merit factor; such flips are counted and must stay rare.
 """
+import subprocess
+from pathlib import Path
+
 import numpy as np
 import pytest
 
-from asteroid_gb300 import api
+from asteroid_gb300 import api, build
 from tests.test_gpu_eval import _vectors, well_conditioned
 
 pytestmark = pytest.mark.gpu
@@ -52,3 +55,21 @@ def test_mixed_fit_finds_same_minimum(gpu, synth_objects):
     assert abs(a.best_f[0] - b.best_f[0]) / a.best_f[0] < 1e-3
     # The mixed fit's reported chi^2 is what FP64 gives at its parameters, within the bar.
     assert abs(f64[0] - b.best_f[0]) / f64[0] <= BAR
+
+
+def test_packed_step_equals_scalar_step(gpu, tmp_path):
+    """The RK4 step on packed FP32x2 pairs gives the scalar double-float step's bits.
+
+    tests/host/packed_step_check.cu restates the step lane by lane with scalar operations and
+    compares sin/cos, both right-hand sides and both steps on 1M random states per configuration
+    (angles up to 2^20 rad, rates up to 2^17 rad/day), on the GPU.  A packed product that the
+    compiler fused into the next packed add, or a lane mix-up, shows up as mismatches."""
+    exe = tmp_path / "packed_step_check"
+    src = Path(__file__).resolve().parent / "host" / "packed_step_check.cu"
+    subprocess.run([build._nvcc(), *build.GENCODE, "-O3", "-std=c++17", f"-I{build.PKG / 'csrc'}",
+                    f"-I{build.INCLUDE}", f"-I{build.PKG / 'host'}", str(src), "-o", str(exe)],
+                   check=True, capture_output=True)
+    r = subprocess.run([str(exe), str(1 << 20)], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True,
+                       timeout=600)
+    print(r.stdout)
+    assert r.returncode == 0, r.stdout
