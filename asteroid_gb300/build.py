@@ -180,6 +180,8 @@ def build_reference_oracle() -> None:
             _run(["bash", str(script), "minima"])
         if not (ORACLE / "_ref" / "ref_ppsi_torque_acc_nofma.cubin").exists():
             _run(["bash", str(script), "nofma"])
+        if not (ORACLE / "_ref" / "libref_nm_c2_nudge_acc.so").exists():
+            _run(["bash", str(script), "nm"])
 
 
 def build(force: bool = False) -> None:

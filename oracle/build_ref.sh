@@ -14,6 +14,11 @@
 #                        oracle/ref_harness_animate.cu: the reference's compute_rgb on the GPU.
 #   ref_<variant>_nofma.cubin  the same device build with nvcc -fmad=false (no multiply-add
 #                        contraction), for the parity check against the engine built the same way.
+#   libref_nm_<variant>.so  the host build above plus the reference's chi2_gpu simplex driver
+#                        (cuda.c:1326-1833) cut from cuda.c and compiled as host code between
+#                        oracle/ref_nm_shim.h and oracle/ref_harness_nm.cu (the block's threads as
+#                        host threads, cuRAND as the engine's Philox stream); -DTIMING, the
+#                        reference's own switch, sets N_STEPS = 100.  Pins the oracle's simplex.
 #
 # The reference's asteroid.h and cuda.c are streamed through sed into nvcc's standard input:
 # the four device functions become __host__ __device__ (host build only), N_FILTERS becomes 8
@@ -87,7 +92,26 @@ if [[ "${1:-all}" == "all" || "${1:-all}" == "cubin" || "${1:-all}" == "nofma" ]
         pids+=($!)
     done
 fi
-[[ "${1:-all}" == "minima" || "${1:-all}" == "animate" || "${1:-all}" == "nofma" ]] && VARIANTS=()
+# name  time_step  macros...  (the simplex driver on the host)
+NM_VARIANTS=(
+  "ppsi_torque_acc 1e-2 -DP_PSI -DTORQUE -DACC"
+  "bc_interp_sp 1e-2 -DBC -DINTERP"
+  "c2_nudge_acc 5e-3 -DP_PSI -DTORQUE -DINTERP -DACC -DNUDGE"
+)
+if [[ "${1:-all}" == "all" || "${1:-all}" == "host" || "${1:-all}" == "nm" ]]; then
+    for v in "${NM_VARIANTS[@]}"; do
+        read -r name ts macros <<<"$v"
+        ( { stream_source "$ts" 1
+            cat "$here/ref_nm_shim.h"
+            awk '/^__global__ void chi2_gpu \(/{p=1} p{print} p&&/^}/{exit}' "$REF/cuda.c"
+            cat "$here/ref_harness_nm.cu"; } |
+          nvcc -x cu -arch=sm_100 -O2 -DMAIN -DTIMING $macros -I"$REF" -I"$here" \
+               -Xcompiler -fPIC,-ffp-contract=off,-ftrivial-auto-var-init=zero,-pthread -shared -w \
+               -o "$OUT/libref_nm_$name.so" - ) &
+        pids+=($!)
+    done
+fi
+[[ "${1:-all}" == "minima" || "${1:-all}" == "animate" || "${1:-all}" == "nofma" || "${1:-all}" == "nm" ]] && VARIANTS=()
 for v in "${VARIANTS[@]}"; do
     read -r name ts macros <<<"$v"
     if [[ "${1:-all}" == "all" || "${1:-all}" == "host" ]]; then

@@ -282,6 +282,49 @@ class RefHost:
         return x
 
 
+class RefNM(RefHost):
+    """The reference's own chi2_gpu simplex driver (cuda.c:1326-1833) run on the host
+    (oracle/_ref/libref_nm_<variant>.so: the block's threads as host threads, cuRAND replaced by
+    the engine's Philox stream, N_STEPS = 100 by the reference's -DTIMING switch)."""
+
+    def __init__(self, variant: str):
+        path = REF_DIR / f"libref_nm_{variant}.so"
+        if not path.exists():
+            raise FileNotFoundError(path)
+        lib = C.CDLL(str(path))
+        V, I = C.c_void_p, C.c_int
+        lib.refnm_fit.restype = I
+        lib.refnm_fit.argtypes = [V, I, V, I, V, I, C.c_float, C.c_float, I, I, V, V, V, V, V, V, V, V, V, I, V, V,
+                                  I, V, I, I, C.c_ulonglong, V, V, V]
+        for n in ("refnm_block_size", "refnm_n_params", "refh_n_params", "refh_n_types"):
+            getattr(lib, n).restype = I
+        lib.refnm_n_steps.restype = C.c_uint
+        self.lib = lib
+        self.n_params = lib.refh_n_params()
+        self.n_types = lib.refh_n_types()
+        self.block_size = lib.refnm_block_size()
+        self.n_steps = lib.refnm_n_steps()
+
+    def fit(self, m, obs, seed, n_blocks, n_stages=1, reopt=False, params0=None):
+        """One chi2_gpu launch of n_blocks blocks: each block's best chi^2, parameters, delta_V."""
+        prop, types, lim = self._tables(m)
+        eph = [np.ascontiguousarray(a, dtype=np.float64) for a in (obs.eph_e, obs.eph_s, obs.eph_mjd0)]
+        p0 = np.ascontiguousarray(params0 if params0 is not None else np.zeros(m.n_params), dtype=np.float64)
+        bf = np.zeros(n_blocks)
+        bp = np.zeros((n_blocks, m.n_params))
+        bdv = np.zeros((n_blocks, obs.n_filters))
+        rc = self.lib.refnm_fit(prop.ctypes.data, m.n_params, types.ctypes.data, m.n_types, lim.ctypes.data,
+                                lim.shape[1], m.ppsi1, m.ppsi2, obs.n_data, obs.n_filters, obs.mjd.ctypes.data,
+                                obs.v.ctypes.data, obs.w.ctypes.data, obs.filt.ctypes.data, obs.e_unit.ctypes.data,
+                                obs.s_unit.ctypes.data, eph[0].ctypes.data, eph[1].ctypes.data, eph[2].ctypes.data,
+                                int(obs.t_min.size), obs.t_min.ctypes.data, obs.v_min.ctypes.data, int(bool(reopt)),
+                                p0.ctypes.data, int(n_blocks), int(n_stages), int(seed), bf.ctypes.data,
+                                bp.ctypes.data, bdv.ctypes.data)
+        if rc:
+            raise RuntimeError(f"refnm_fit failed ({rc}): tables or sizes do not match the reference build")
+        return {"best_f": bf, "best_params": bp, "best_dv": bdv}
+
+
 def ref_render(geo):
     """The reference's own compute_rgb on the GPU (oracle/_ref/ref_animate.cubin), 1080 x 1080."""
     cubin = REF_DIR / "ref_animate.cubin"
