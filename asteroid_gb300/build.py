@@ -180,7 +180,8 @@ def build_reference_oracle() -> None:
             _run(["bash", str(script), "minima"])
         if not (ORACLE / "_ref" / "ref_ppsi_torque_acc_nofma.cubin").exists():
             _run(["bash", str(script), "nofma"])
-        if not (ORACLE / "_ref" / "libref_nm_c2_nudge_acc.so").exists():
+        if not all((ORACLE / "_ref" / f"libref_nm_{v}.so").exists()
+                   for v in ("c2_nudge_acc", "rmsd_bc_interp_sp", "rmsd_sph_ppsi_torque_acc")):
             _run(["bash", str(script), "nm"])
 
 

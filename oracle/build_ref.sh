@@ -93,19 +93,30 @@ if [[ "${1:-all}" == "all" || "${1:-all}" == "cubin" || "${1:-all}" == "nofma" ]
     done
 fi
 # name  time_step  macros...  (the simplex driver on the host)
+# (the -DRMSD variants take chi2_gpu_rms, the others chi2_gpu)
 NM_VARIANTS=(
   "ppsi_torque_acc 1e-2 -DP_PSI -DTORQUE -DACC"
   "bc_interp_sp 1e-2 -DBC -DINTERP"
   "c2_nudge_acc 5e-3 -DP_PSI -DTORQUE -DINTERP -DACC -DNUDGE"
+  "rmsd_ppsi_torque_acc 1e-2 -DP_PSI -DTORQUE -DACC -DRMSD"
+  "rmsd_sph_ppsi_torque_acc 1e-2 -DP_PSI -DTORQUE -DACC -DRMSD -DSPHERICAL_K"
+  "rmsd_bc_interp_sp 1e-2 -DBC -DINTERP -DRMSD"
 )
 if [[ "${1:-all}" == "all" || "${1:-all}" == "host" || "${1:-all}" == "nm" ]]; then
     for v in "${NM_VARIANTS[@]}"; do
         read -r name ts macros <<<"$v"
+        kernel=chi2_gpu
+        [[ "$macros" == *-DRMSD* ]] && kernel=chi2_gpu_rms
         ( { stream_source "$ts" 1
             cat "$here/ref_nm_shim.h"
-            awk '/^__global__ void chi2_gpu \(/{p=1} p{print} p&&/^}/{exit}' "$REF/cuda.c"
+            # from the kernel's first line to its closing brace (chi2_gpu_rms: the line before its
+            # "#endif //RMSD", the brace being indented there)
+            awk -v k="$kernel" '$0 ~ "^__global__ void " k " \\(" {p=1}
+                                p && k == "chi2_gpu_rms" && /^ *#endif *\/\/ *RMSD/ {exit}
+                                p {print}
+                                p && k == "chi2_gpu" && /^}/ {exit}' "$REF/cuda.c"
             cat "$here/ref_harness_nm.cu"; } |
-          nvcc -x cu -arch=sm_100 -O2 -DMAIN -DTIMING $macros -I"$REF" -I"$here" \
+          nvcc -x cu -arch=sm_100 -O2 -DMAIN -DTIMING $macros -I"$REF" -I"$here" -I"$here/../asteroid_gb300/csrc" \
                -Xcompiler -fPIC,-ffp-contract=off,-ftrivial-auto-var-init=zero,-pthread -shared -w \
                -o "$OUT/libref_nm_$name.so" - ) &
         pids+=($!)

@@ -293,9 +293,10 @@ class RefNM(RefHost):
             raise FileNotFoundError(path)
         lib = C.CDLL(str(path))
         V, I = C.c_void_p, C.c_int
-        lib.refnm_fit.restype = I
-        lib.refnm_fit.argtypes = [V, I, V, I, V, I, C.c_float, C.c_float, I, I, V, V, V, V, V, V, V, V, V, I, V, V,
-                                  I, V, I, I, C.c_ulonglong, V, V, V]
+        if hasattr(lib, "refnm_fit"):  # the -DRMSD builds hold refnm_rmsd instead
+            lib.refnm_fit.restype = I
+            lib.refnm_fit.argtypes = [V, I, V, I, V, I, C.c_float, C.c_float, I, I, V, V, V, V, V, V, V, V, V, I, V,
+                                      V, I, V, I, I, C.c_ulonglong, V, V, V]
         for n in ("refnm_block_size", "refnm_n_params", "refh_n_params", "refh_n_types"):
             getattr(lib, n).restype = I
         lib.refnm_n_steps.restype = C.c_uint
@@ -323,6 +324,34 @@ class RefNM(RefHost):
         if rc:
             raise RuntimeError(f"refnm_fit failed ({rc}): tables or sizes do not match the reference build")
         return {"best_f": bf, "best_params": bp, "best_dv": bdv}
+
+    def rmsd(self, m, obs, params0, seed, call, n_blocks, samples, dx, reopt=1):
+        """One chi2_gpu_rms launch (-DRMSD builds): f0 and f1 (float, as d_f0 / d_f1), the counts
+        of evaluated and rejected points, and the parameter ranges over all blocks (float)."""
+        lib = self.lib
+        if not hasattr(lib, "refnm_rmsd"):
+            raise RuntimeError("not a -DRMSD build")
+        V, I = C.c_void_p, C.c_int
+        lib.refnm_rmsd.restype = I
+        lib.refnm_rmsd.argtypes = [V, I, V, I, V, I, I, I, V, V, V, V, V, V, V, V, V, I, V, I, I, C.c_float,
+                                   C.c_ulonglong, C.c_uint, V, V, V, V]
+        prop, types, lim = self._tables(m)
+        eph = [np.ascontiguousarray(a, dtype=np.float64) for a in (obs.eph_e, obs.eph_s, obs.eph_mjd0)]
+        p0 = np.ascontiguousarray(params0, dtype=np.float64)
+        f01 = np.zeros(2)
+        counts = np.zeros(2, np.int64)
+        pmin = np.zeros(m.n_params, np.float32)
+        pmax = np.zeros(m.n_params, np.float32)
+        rc = lib.refnm_rmsd(prop.ctypes.data, m.n_params, types.ctypes.data, m.n_types, lim.ctypes.data, lim.shape[1],
+                            obs.n_data, obs.n_filters, obs.mjd.ctypes.data, obs.v.ctypes.data, obs.w.ctypes.data,
+                            obs.filt.ctypes.data, obs.e_unit.ctypes.data, obs.s_unit.ctypes.data, eph[0].ctypes.data,
+                            eph[1].ctypes.data, eph[2].ctypes.data, int(reopt), p0.ctypes.data, int(n_blocks),
+                            int(samples), float(dx), int(seed), int(call), f01.ctypes.data, counts.ctypes.data,
+                            pmin.ctypes.data, pmax.ctypes.data)
+        if rc:
+            raise RuntimeError(f"refnm_rmsd failed ({rc}): tables or sizes do not match the reference build")
+        return {"f0": f01[0], "f1": f01[1], "n_tot": int(counts[0]), "n_bad": int(counts[1]), "par_min": pmin,
+                "par_max": pmax}
 
 
 def ref_render(geo):

@@ -1,31 +1,37 @@
 /*
  * ref_nm_shim.h -- TEST INFRASTRUCTURE ONLY.  Lets the text of the reference's chi2_gpu kernel
- * (cuda.c:1326-1833, the downhill-simplex driver) compile and run as host code, so that the
- * oracle's restatement of it (nm_oracle_body.h, nm_oracle_impl.h) can be pinned to the
- * reference's own code on the CPU.
+ * (cuda.c:1326-1833, the downhill-simplex driver) or chi2_gpu_rms kernel (cuda.c:2148-2389, the
+ * RMSD confidence-interval sampler) compile and run as host code, so that the oracle's
+ * restatements of them (nm_oracle_*.h, rmsd_oracle*.h) can be pinned to the reference's own
+ * code on the CPU.
  *
  * oracle/build_ref.sh streams, into one translation unit: the reference's asteroid.h and cuda.c
  * (as for libref_<variant>.so, chi2one / x2params / params2x re-qualified __host__ __device__),
- * this header, the chi2_gpu function cut from cuda.c, and ref_harness_nm.cu, which undoes the
- * macros below and provides the entry point.  Nothing of the reference is written to disk.
+ * this header, the kernel cut from cuda.c, and ref_harness_nm.cu, which undoes the macros below
+ * and provides the entry point.  Nothing of the reference is written to disk.
  *
  * The CUDA execution model of one block, on the host:
  *   - a block's BSIZE threads are BSIZE host threads; __syncthreads() is a barrier among them;
  *   - __shared__ variables become function-static, i.e. one copy shared by the block's threads
- *     (blocks run one after the other);
+ *     (blocks run one after the other); atomicAdd is a locked host add;
  *   - threadIdx / blockIdx / blockDim are per-thread (thread_local) values;
- *   - the __device__ tables the kernel reads (dLimits, dTypes, dProperty, d_x2_params,
- *     d_chi2_params, d_params0, the INTERP ephemeris) are host arrays that the entry point fills;
- *   - curandState / curand_uniform is the engine's Philox stream: draw k of stage s of chain c is
- *     uniform01(seed, c, s, k) (philox.cuh).  The kernel draws exactly 3 N_PARAMS numbers per
- *     stage (N_PARAMS for the start point, two for each further vertex, cuda.c:1462,1519,1523),
- *     so the stage and the draw index follow from the running count of draws.
- * With the reference's own cuRAND XORWOW states replaced by these draws, the kernel's chains take
- * the same start points as the oracle's and the engine's, and every later step is the reference's.
+ *   - the __device__ variables the kernels read or write (dLimits, dTypes, dProperty, d_x2_params,
+ *     d_chi2_params, d_params0, the INTERP ephemeris, d_Ntot, d_Nbad, d_f0, d_f1) are host
+ *     variables that the entry point fills and reads;
+ *   - curandState / curand_uniform / curand_normal is the engine's Philox stream (philox.cuh):
+ *     chi2_gpu draws exactly 3 N_PARAMS uniforms per stage (N_PARAMS for the start point, two
+ *     for each further vertex, cuda.c:1462,1519,1523), so draw k of stage s of thread c is
+ *     uniform01(seed, c, s, k); chi2_gpu_rms draws exactly N_PARAMS normals per sample
+ *     (cuda.c:2277), so normal i of sample k of thread c is element i mod 4 of
+ *     normal4(seed, c, 0x80000000 | call, k ceil(N_PARAMS / 4) + i / 4).  Both follow from the
+ *     running count of draws.
+ * With the reference's own cuRAND XORWOW states replaced by these draws, the kernels take the
+ * same random points as the oracle and the engine, and every other step is the reference's.
  */
 #include <stdint.h>
 #include <condition_variable>
 #include <mutex>
+#include "philox.cuh"
 
 namespace refnm {
 
@@ -57,35 +63,37 @@ struct Barrier {
 };
 static Barrier barrier;
 
-/* Philox4x32-10 (Salmon et al., SC'11), as in philox.cuh. */
-static inline void philox(uint32_t c[4], uint32_t k0, uint32_t k1)
-{
-    for (int r = 0; r < 10; r++) {
-        const uint64_t p0 = (uint64_t)0xD2511F53u * c[0], p1 = (uint64_t)0xCD9E8D57u * c[2];
-        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ k0, n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ k1;
-        c[0] = n0;
-        c[1] = (uint32_t)p1;
-        c[2] = n2;
-        c[3] = (uint32_t)p0;
-        k0 += 0x9E3779B9u;
-        k1 += 0xBB67AE85u;
-    }
-}
-
 struct Rng {
     uint64_t seed, chain;
-    uint32_t count;  /* draws so far */
-    int per_stage;   /* 3 N_PARAMS */
+    uint32_t count;    /* draws so far */
+    int per_stage;     /* chi2_gpu: 3 N_PARAMS uniforms per stage; chi2_gpu_rms: N_PARAMS normals per sample */
+    uint32_t call;     /* chi2_gpu_rms: the launch's index in the host loop */
 };
 
 static inline float uniform(Rng* s)
 {
     const uint32_t stage = s->count / (uint32_t)s->per_stage, k = s->count % (uint32_t)s->per_stage;
     s->count++;
-    uint32_t c[4] = {k >> 2, stage, (uint32_t)s->chain, (uint32_t)(s->chain >> 32)};
-    philox(c, (uint32_t)s->seed, (uint32_t)(s->seed >> 32));
-    const uint32_t u = c[k & 3];
-    return ((float)(u >> 8) + 0.5f) * (1.0f / 16777216.0f);
+    return ast::uniform01(s->seed, s->chain, stage, k);
+}
+
+static inline float normal(Rng* s)
+{
+    const uint32_t k = s->count / (uint32_t)s->per_stage, i = s->count % (uint32_t)s->per_stage;
+    const uint32_t nq = ((uint32_t)s->per_stage + 3u) / 4u;
+    s->count++;
+    float z[4];
+    ast::normal4(s->seed, s->chain, 0x80000000u | s->call, k * nq + i / 4u, z);
+    return z[i % 4u];
+}
+
+static std::mutex atomic_lock;
+static inline int atomic_add(int* p, int v)
+{
+    std::lock_guard<std::mutex> g(atomic_lock);
+    const int old = *p;
+    *p = old + v;
+    return old;
 }
 
 }  // namespace refnm
@@ -99,6 +107,8 @@ static struct chi2_struct refnm_d_chi2_params;
 static double refnm_d_params0[N_PARAMS];
 static double refnm_dE_x0[3], refnm_dE_y0[3], refnm_dE_z0[3], refnm_dS_x0[3], refnm_dS_y0[3], refnm_dS_z0[3],
     refnm_dMJD0[3];
+static int refnm_d_Ntot, refnm_d_Nbad;
+static float refnm_d_f0, refnm_d_f1;
 
 #pragma push_macro("__global__")
 #pragma push_macro("__shared__")
@@ -112,7 +122,14 @@ static double refnm_dE_x0[3], refnm_dE_y0[3], refnm_dE_z0[3], refnm_dS_x0[3], re
 #define __syncthreads() refnm::barrier.wait()
 #define curandState refnm::Rng
 #define curand_uniform(s) refnm::uniform(s)
+#define curand_normal(s) refnm::normal(s)
+#define atomicAdd refnm::atomic_add
 #define chi2_gpu refnm_chi2_gpu
+#define chi2_gpu_rms refnm_chi2_gpu_rms
+#define d_Ntot refnm_d_Ntot
+#define d_Nbad refnm_d_Nbad
+#define d_f0 refnm_d_f0
+#define d_f1 refnm_d_f1
 #define dLimits refnm_dLimits
 #define dTypes refnm_dTypes
 #define dProperty refnm_dProperty
