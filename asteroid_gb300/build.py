@@ -173,15 +173,20 @@ def build_reference_oracle() -> None:
     script = ORACLE / "build_ref.sh"
     ref = Path(os.environ.get("AST_REFERENCE_DIR", str(ROOT.parent / "reference")))
     if script.exists() and (ref / "cuda.c").exists():
-        have = list((ORACLE / "_ref").glob("libref_*.so")) if (ORACLE / "_ref").exists() else []
+        R = ORACLE / "_ref"
+        have = list(R.glob("libref_*.so")) if R.exists() else []
         if not have:
             _run(["bash", str(script)])
-        elif not (ORACLE / "_ref" / "libref_minima.so").exists():
+            return
+        if not (R / "libref_minima.so").exists():
             _run(["bash", str(script), "minima"])
-        if not (ORACLE / "_ref" / "ref_ppsi_torque_acc_nofma.cubin").exists():
+        if not (R / "ref_ppsi_torque_acc_nofma.cubin").exists():
             _run(["bash", str(script), "nofma"])
-        if not all((ORACLE / "_ref" / f"libref_nm_{v}.so").exists()
-                   for v in ("c2_nudge_acc", "rmsd_bc_interp_sp", "rmsd_sph_ppsi_torque_acc")):
+        # The host builds again when their harness is newer than them (new entry points).
+        if _stale(R / "libref_ppsi_torque_acc.so", [ORACLE / "ref_harness_host.cu", script]):
+            _run(["bash", str(script), "host"])  # also the simplex / RMSD drivers
+        elif any(_stale(R / f"libref_nm_{v}.so", [ORACLE / "ref_nm_shim.h", ORACLE / "ref_harness_nm.cu"])
+                 for v in ("ppsi_torque_acc", "c2_nudge_acc", "rmsd_bc_interp_sp", "rmsd_sph_ppsi_torque_acc")):
             _run(["bash", str(script), "nm"])
 
 

@@ -261,6 +261,25 @@ class RefHost:
             raise RuntimeError(f"refh_chi2 failed ({rc}): tables do not match the reference build")
         return out[0], dv
 
+    def model_curve(self, m, obs, params):
+        """chi2one with Nplot > 0 (the plot branch, cuda.c:699-704): the model magnitude at every
+        observation, without the delta_V shift.  Not available in -DNUDGE builds."""
+        prop, types, lim = self._tables(m)
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        out = np.zeros(obs.n_data)
+        V, I = C.c_void_p, C.c_int
+        f = self.lib.refh_model_curve
+        f.restype = I
+        f.argtypes = [V, I, V, I, V, I, I, I, V, V, V, V, V, V, V, V, V, V, V]
+        rc = f(prop.ctypes.data, m.n_params, types.ctypes.data, m.n_types, lim.ctypes.data, lim.shape[1], obs.n_data,
+               obs.n_filters, obs.mjd.ctypes.data, obs.v.ctypes.data, obs.w.ctypes.data, obs.filt.ctypes.data,
+               obs.e_unit.ctypes.data, obs.s_unit.ctypes.data, np.ascontiguousarray(obs.eph_e).ctypes.data,
+               np.ascontiguousarray(obs.eph_s).ctypes.data, np.ascontiguousarray(obs.eph_mjd0).ctypes.data,
+               p.ctypes.data, out.ctypes.data)
+        if rc:
+            raise RuntimeError(f"refh_model_curve failed ({rc})")
+        return out
+
     def x2params(self, m, x, reopt=1):
         prop, types, lim = self._tables(m)
         xx = np.ascontiguousarray(x, dtype=np.float64)

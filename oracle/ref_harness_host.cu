@@ -116,3 +116,50 @@ extern "C" int refh_params2x(const int* property, int n_params, const int* types
     for (int i = 0; i < N_PARAMS; i++) x[i] = (double)xc[i];
     return 0;
 }
+
+/* chi2one with Nplot > 0 on one parameter vector (the model-curve branch that chi2_plot calls,
+ * cuda.c:699-704, cuda.c:1945): the reference writes Vmod + delta_V[0] into d_Vmod, whose host
+ * copy this build reads back; with delta_V[0] = 0 that is the model magnitude itself.  Not for
+ * -DNUDGE builds (the reference's NUDGE code does not support the plot branch, cuda.c:1936). */
+extern "C" int refh_model_curve(const int* property, int n_params, const int* types, int n_types,
+                                const double* limits, int max_types,
+                                int n_data, int n_filters, const double* mjd, const float* v, const float* w,
+                                const int* filt, const double* e_unit, const double* s_unit,
+                                const double* eph_e /* [3][3] */, const double* eph_s, const double* eph_mjd0,
+                                const double* params, double* vmod)
+{
+#ifdef NUDGE
+    return -4;
+#endif
+    if (refh_load_tables(property, n_params, types, n_types, limits, max_types)) return -1;
+    if (n_filters > N_FILTERS) return -2;
+    if (n_data > NPLOT) return -3;
+    struct obs_data* data = (struct obs_data*)calloc((size_t)n_data, sizeof(struct obs_data));
+    for (int i = 0; i < n_data; i++) {
+        data[i].V = v[i];
+        data[i].w = w[i];
+        data[i].MJD = mjd[i];
+        data[i].Filter = filt[i];
+#ifndef INTERP
+        data[i].E_x = e_unit[3 * i]; data[i].E_y = e_unit[3 * i + 1]; data[i].E_z = e_unit[3 * i + 2];
+        data[i].S_x = s_unit[3 * i]; data[i].S_y = s_unit[3 * i + 1]; data[i].S_z = s_unit[3 * i + 2];
+#endif
+    }
+    struct chi2_struct sp;
+    memset(&sp, 0, sizeof(sp));
+#ifdef INTERP
+    for (int k = 0; k < 3; k++) {
+        sp.E_x0[k] = eph_e[0 * 3 + k]; sp.E_y0[k] = eph_e[1 * 3 + k]; sp.E_z0[k] = eph_e[2 * 3 + k];
+        sp.S_x0[k] = eph_s[0 * 3 + k]; sp.S_y0[k] = eph_s[1 * 3 + k]; sp.S_z0[k] = eph_s[2 * 3 + k];
+        sp.MJD0[k] = eph_mjd0[k];
+    }
+#endif
+    double p[N_PARAMS];
+    for (int i = 0; i < N_PARAMS; i++) p[i] = params[i];
+    CHI_FLOAT dv[N_FILTERS];
+    for (int m = 0; m < N_FILTERS; m++) dv[m] = 0;
+    chi2one(p, data, n_data, n_filters, dv, n_data, &sp, h_types);
+    for (int i = 0; i < n_data; i++) vmod[i] = d_Vmod[i];
+    free(data);
+    return 0;
+}

@@ -103,3 +103,21 @@ def test_oracle_random_vectors_against_reference_build(built, oracle_mod, path):
             assert np.array_equal(d1, d2[: obs.n_filters], equal_nan=True)
             n += 1
     assert n > 20
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=[p.stem for p in FIXTURES])
+def test_oracle_model_curve_matches_reference_plot_branch(built, oracle_mod, path):
+    """The model curve (chi2one with Nplot > 0, the branch chi2_plot and the -plot mode use,
+    cuda.c:699-704) from the reference's host build equals the oracle's, bit for bit, for every
+    fixture parameter vector (the reference does not support the branch under NUDGE)."""
+    fx, m, obs = load_fixture(path)
+    lib = REF_DIR / f"libref_{fx['variant']}.so"
+    if not lib.exists() or not EXACT:
+        pytest.skip("reference host build not present (it is built where the reference checkout exists)")
+    if "NUDGE" in fx["flags"]:
+        pytest.skip("the reference's plot branch is not defined under NUDGE")
+    ref = oracle_mod.RefHost(fx["variant"])
+    for p in fx["params"]:
+        a = ref.model_curve(m, obs, np.array(p))
+        b = oracle_mod.model_curve(m, obs, np.array(p))
+        assert np.array_equal(a, b, equal_nan=True)
