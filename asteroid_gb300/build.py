@@ -186,7 +186,9 @@ def build_reference_oracle() -> None:
         if _stale(R / "libref_ppsi_torque_acc.so", [ORACLE / "ref_harness_host.cu", script]):
             _run(["bash", str(script), "host"])  # also the simplex / RMSD drivers
         elif any(_stale(R / f"libref_nm_{v}.so", [ORACLE / "ref_nm_shim.h", ORACLE / "ref_harness_nm.cu"])
-                 for v in ("ppsi_torque_acc", "c2_nudge_acc", "rmsd_bc_interp_sp", "rmsd_sph_ppsi_torque_acc")):
+                 for v in ("ppsi_torque_acc", "ppsi_torque_sp", "torque_interp_acc", "bc_interp_acc", "bw_torque_acc",
+                           "bc_torque_ppsi_acc", "free_acc", "bc_interp_sp", "c2_nudge_acc", "rmsd_ppsi_torque_acc",
+                           "rmsd_bc_interp_sp", "rmsd_sph_ppsi_torque_acc")):
             _run(["bash", str(script), "nm"])
 
 

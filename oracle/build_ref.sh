@@ -96,6 +96,12 @@ fi
 # (the -DRMSD variants take chi2_gpu_rms, the others chi2_gpu)
 NM_VARIANTS=(
   "ppsi_torque_acc 1e-2 -DP_PSI -DTORQUE -DACC"
+  "ppsi_torque_sp 1e-2 -DP_PSI -DTORQUE"
+  "torque_interp_acc 1e-2 -DTORQUE -DINTERP -DACC"
+  "bc_interp_acc 1e-2 -DBC -DINTERP -DACC"
+  "bw_torque_acc 1e-2 -DBW_BALL -DTORQUE -DACC"
+  "bc_torque_ppsi_acc 1e-2 -DBC -DTORQUE -DP_PSI -DACC"
+  "free_acc 1e-2 -DACC"
   "bc_interp_sp 1e-2 -DBC -DINTERP"
   "c2_nudge_acc 5e-3 -DP_PSI -DTORQUE -DINTERP -DACC -DNUDGE"
   "rmsd_ppsi_torque_acc 1e-2 -DP_PSI -DTORQUE -DACC -DRMSD"

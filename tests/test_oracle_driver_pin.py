@@ -9,9 +9,10 @@ Everything else is the reference's code.
 Simplex: the random start rules, the simplex steps, the block's serial argmin, the P_PSI
 re-meaning of x at the stage hand-off, the final x2params and delta_V.  The oracle
 (oracle/nm_oracle_*.h, whose chains the GPU fit kernel follows in tests/test_gpu_fit.py) must give
-the same block results bit for bit: two stages of 2 x 256 chains of N_STEPS = 100 (the
-reference's -DTIMING value), random and -reopt starts, on the fixture objects of two variants and
-on a 400-point NUDGE object (the fixture's 120 points give no admissible minima: every chain would
+the same block results bit for bit: two stages of a block of 256 chains of N_STEPS = 100 (the
+reference's -DTIMING value), random and -reopt starts, on the fixture objects of eight variants
+(every non-RMSD fixture: P_PSI, TORQUE, INTERP, BC, BW_BALL, free rotation; CHI_FLOAT double and
+float) and on a 400-point NUDGE object (the fixture's 120 points give no admissible minima: every chain would
 end at the 1e30 penalty).
 
 RMSD: the normal-draw perturbation with its hard-limit clamps, x2params, the one-sigma RMSD test,
@@ -31,8 +32,8 @@ REF_DIR = Path(__file__).resolve().parents[1] / "oracle" / "_ref"
 
 def _compare(oracle_mod, variant, m, obs, reopt, p0):
     ref = oracle_mod.RefNM(variant)
-    a = ref.fit(m, obs, seed=5, n_blocks=2, n_stages=2, reopt=reopt, params0=p0)
-    b = oracle_mod.fit(m, obs, seed=5, n_chains=2 * ref.block_size, group_size=ref.block_size, n_stages=2,
+    a = ref.fit(m, obs, seed=5, n_blocks=1, n_stages=2, reopt=reopt, params0=p0)
+    b = oracle_mod.fit(m, obs, seed=5, n_chains=ref.block_size, group_size=ref.block_size, n_stages=2,
                        reopt=reopt, params0=p0, steps_cap=ref.n_steps)
     print(variant, "reopt" if reopt else "random", "block best chi2", a["best_f"])
     assert np.all(a["best_f"] < 1e29)
@@ -46,7 +47,8 @@ def _need(variant):
         pytest.skip("reference simplex host build not present (it is built where the reference checkout exists)")
 
 
-@pytest.mark.parametrize("variant", ["ppsi_torque_acc", "bc_interp_sp"])
+@pytest.mark.parametrize("variant", ["ppsi_torque_acc", "ppsi_torque_sp", "torque_interp_acc", "bc_interp_acc",
+                                     "bw_torque_acc", "bc_torque_ppsi_acc", "free_acc", "bc_interp_sp"])
 @pytest.mark.parametrize("reopt", [False, True], ids=["random", "reopt"])
 def test_oracle_simplex_equals_reference_chi2_gpu(built, oracle_mod, variant, reopt):
     _need(variant)
