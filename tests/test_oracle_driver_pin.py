@@ -19,13 +19,19 @@ RMSD: the normal-draw perturbation with its hard-limit clamps, x2params, the one
 the periodic-angle and SPHERICAL_K conversions and the float min/max reductions.  The oracle
 (oracle/rmsd_oracle*.h, which the GPU sampler matches in tests/test_rmsd.py) must give the same
 f0, f1, sample counts and parameter ranges bit for bit, for two launch indices of the host loop.
+
+tests/golden/ref_drivers.json (tests/golden/make_driver_golden.py) keeps the reference builds'
+results for the fixture objects, so the oracle is checked against them where the reference is
+absent too (bit for bit on x86-64, where they were generated; to 1e-12 elsewhere).
 """
 from pathlib import Path
 
 import numpy as np
 import pytest
 
-from tests.test_oracle_pin import EXACT, GOLDEN, load_fixture
+import json
+
+from tests.test_oracle_pin import EXACT, GOLDEN, load_fixture, same
 
 REF_DIR = Path(__file__).resolve().parents[1] / "oracle" / "_ref"
 
@@ -84,3 +90,31 @@ def test_oracle_rmsd_equals_reference_chi2_gpu_rms(built, oracle_mod, variant, f
         assert np.float32(b["f0"]) == np.float32(a["f0"]) and np.float32(b["f1"]) == np.float32(a["f1"])
         assert np.array_equal(np.float32(b["par_min"]), a["par_min"])
         assert np.array_equal(np.float32(b["par_max"]), a["par_max"])
+
+
+DRIVERS = json.loads((GOLDEN / "ref_drivers.json").read_text())
+
+
+@pytest.mark.parametrize("case", DRIVERS["simplex"],
+                         ids=[f"{c['fixture']}-{'reopt' if c['reopt'] else 'random'}" for c in DRIVERS["simplex"]])
+def test_oracle_simplex_matches_reference_golden(built, oracle_mod, case):
+    fx, m, obs = load_fixture(GOLDEN / f"ref_{case['fixture']}.json")
+    p0 = None if case["params0"] is None else np.array(case["params0"])
+    b = oracle_mod.fit(m, obs, seed=case["seed"], n_chains=case["n_chains"], group_size=case["n_chains"],
+                       n_stages=case["n_stages"], reopt=case["reopt"], params0=p0, steps_cap=case["steps_cap"])
+    assert same(b["best_f"], case["best_f"])
+    assert same(b["best_params"], case["best_params"])
+    assert same(b["best_dv"], case["best_dv"])
+
+
+@pytest.mark.parametrize("case", DRIVERS["rmsd"], ids=[f"{c['build']}-call{c['call']}" for c in DRIVERS["rmsd"]])
+def test_oracle_rmsd_matches_reference_golden(built, oracle_mod, case):
+    fx, m, obs = load_fixture(GOLDEN / f"ref_{case['fixture']}.json")
+    b = oracle_mod.rmsd(m, obs, np.array(case["params0"]), seed=case["seed"], call=case["call"],
+                        n_streams=case["n_streams"], samples=case["samples"], dx=case["dx"], reopt=1,
+                        spherical=case["spherical"])
+    f32 = lambda v: np.float32(np.asarray(v, dtype=np.float64)).astype(np.float64)
+    assert same(f32([b["f0"], b["f1"]]), [case["f0"], case["f1"]])
+    assert same(f32(b["par_min"]), case["par_min"]) and same(f32(b["par_max"]), case["par_max"])
+    if EXACT:
+        assert (b["n_tot"], b["n_bad"]) == (case["n_tot"], case["n_bad"])
