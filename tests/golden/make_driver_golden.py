@@ -1,4 +1,4 @@
-"""Generate tests/golden/ref_drivers.json from the reference's own chi2_gpu and chi2_gpu_rms.
+"""Generate tests/golden/drivers_ref.json from the reference's own chi2_gpu and chi2_gpu_rms.
 
 Run here, where the reference checkout exists:  bash oracle/build_ref.sh nm && python
 tests/golden/make_driver_golden.py.  For every host build of the reference's simplex driver and
@@ -66,7 +66,7 @@ def main() -> int:
                                 "par_min": [float(v) for v in r["par_min"]],
                                 "par_max": [float(v) for v in r["par_max"]]})
             print(build, call, r["n_tot"], r["n_bad"])
-    (GOLDEN / "ref_drivers.json").write_text(json.dumps(out, indent=1))
+    (GOLDEN / "drivers_ref.json").write_text(json.dumps(out, indent=1))
     return 0
 
 

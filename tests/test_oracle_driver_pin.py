@@ -20,7 +20,7 @@ the periodic-angle and SPHERICAL_K conversions and the float min/max reductions.
 (oracle/rmsd_oracle*.h, which the GPU sampler matches in tests/test_rmsd.py) must give the same
 f0, f1, sample counts and parameter ranges bit for bit, for two launch indices of the host loop.
 
-tests/golden/ref_drivers.json (tests/golden/make_driver_golden.py) keeps the reference builds'
+tests/golden/drivers_ref.json (tests/golden/make_driver_golden.py) keeps the reference builds'
 results for the fixture objects, so the oracle is checked against them where the reference is
 absent too (bit for bit on x86-64, where they were generated; to 1e-12 elsewhere).
 """
@@ -92,7 +92,7 @@ def test_oracle_rmsd_equals_reference_chi2_gpu_rms(built, oracle_mod, variant, f
         assert np.array_equal(np.float32(b["par_max"]), a["par_max"])
 
 
-DRIVERS = json.loads((GOLDEN / "ref_drivers.json").read_text())
+DRIVERS = json.loads((GOLDEN / "drivers_ref.json").read_text())
 
 
 @pytest.mark.parametrize("case", DRIVERS["simplex"],
