@@ -96,10 +96,18 @@ DRIVERS = json.loads((GOLDEN / "drivers_ref.json").read_text())
 
 
 @pytest.mark.parametrize("case", DRIVERS["simplex"],
-                         ids=[f"{c['fixture']}-{'reopt' if c['reopt'] else 'random'}" for c in DRIVERS["simplex"]])
-def test_oracle_simplex_matches_reference_golden(built, oracle_mod, case):
-    fx, m, obs = load_fixture(GOLDEN / f"ref_{case['fixture']}.json")
-    p0 = None if case["params0"] is None else np.array(case["params0"])
+                         ids=[f"{c.get('fixture', 'nudge400')}-{'reopt' if c['reopt'] else 'random'}"
+                              for c in DRIVERS["simplex"]])
+def test_oracle_simplex_matches_reference_golden(built, oracle_mod, case, tmp_path):
+    if "synth" in case:
+        from asteroid_gb300 import synth
+
+        cfg = synth.SynthConfig(**{k: tuple(v) if isinstance(v, list) else v for k, v in case["synth"].items()})
+        s = synth.generate(cfg, tmp_path / cfg.name, vmod_fn=lambda m, o, p: oracle_mod.model_curve(m, o, p))
+        m, obs, p0 = s.model, s.obs, s.params_true
+    else:
+        fx, m, obs = load_fixture(GOLDEN / f"ref_{case['fixture']}.json")
+        p0 = None if case["params0"] is None else np.array(case["params0"])
     b = oracle_mod.fit(m, obs, seed=case["seed"], n_chains=case["n_chains"], group_size=case["n_chains"],
                        n_stages=case["n_stages"], reopt=case["reopt"], params0=p0, steps_cap=case["steps_cap"])
     assert same(b["best_f"], case["best_f"])
