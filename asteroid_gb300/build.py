@@ -182,6 +182,9 @@ def build_reference_oracle() -> None:
             _run(["bash", str(script), "minima"])
         if not (R / "ref_ppsi_torque_acc_nofma.cubin").exists():
             _run(["bash", str(script), "nofma"])
+        if any(_stale(R / f"libref_read_{v}.so", [ORACLE / "ref_harness_read_data.cu"])
+               for v in ("plain", "interp", "interp_nudge")):
+            _run(["bash", str(script), "read"])
         # The host builds again when their harness is newer than them (new entry points).
         if _stale(R / "libref_ppsi_torque_acc.so", [ORACLE / "ref_harness_host.cu", script]):
             _run(["bash", str(script), "host"])  # also the simplex / RMSD drivers

@@ -19,6 +19,9 @@
 #                        oracle/ref_nm_shim.h and oracle/ref_harness_nm.cu (the block's threads as
 #                        host threads, cuRAND as the engine's Philox stream); -DTIMING, the
 #                        reference's own switch, sets N_STEPS = 100.  Pins the oracle's simplex.
+#   libref_read_<variant>.so  the reference's host readers, read_data.c and misc.c, with
+#                        oracle/ref_harness_read_data.cu (cudaMallocHost as malloc); pins the
+#                        engine's C reader (host/read_data.c, host/misc.c).
 #
 # The reference's asteroid.h and cuda.c are streamed through sed into nvcc's standard input:
 # the four device functions become __host__ __device__ (host build only), N_FILTERS becomes 8
@@ -128,7 +131,27 @@ if [[ "${1:-all}" == "all" || "${1:-all}" == "host" || "${1:-all}" == "nm" ]]; t
         pids+=($!)
     done
 fi
-[[ "${1:-all}" == "minima" || "${1:-all}" == "animate" || "${1:-all}" == "nofma" || "${1:-all}" == "nm" ]] && VARIANTS=()
+# name  macros...  (the host readers: read_data.c and misc.c)
+READ_VARIANTS=(
+  "plain"
+  "interp -DINTERP"
+  "interp_nudge -DINTERP -DNUDGE"
+)
+if [[ -f "$REF/read_data.c" && -f "$REF/misc.c" && ( "${1:-all}" == "all" || "${1:-all}" == "host" || "${1:-all}" == "read" ) ]]; then
+    for v in "${READ_VARIANTS[@]}"; do
+        read -r name macros <<<"$v"
+        ( { sed -e 's/^const int N_FILTERS = 1;/const int N_FILTERS = 8;/' "$REF/asteroid.h"
+            cat "$here/ref_harness_read_data.cu"
+            sed -e 's/^#include "asteroid.h"//' "$REF/read_data.c"
+            sed -e 's/^#include "asteroid.h"//' "$REF/misc.c"
+            echo "#define REFR_TAIL 1"
+            cat "$here/ref_harness_read_data.cu"; } |
+          nvcc -x cu -arch=sm_100 -O2 -DMAIN $macros -I"$REF" -Xcompiler -fPIC,-ffp-contract=off -shared -w \
+               -o "$OUT/libref_read_$name.so" - ) &
+        pids+=($!)
+    done
+fi
+[[ "${1:-all}" == "minima" || "${1:-all}" == "animate" || "${1:-all}" == "nofma" || "${1:-all}" == "nm" || "${1:-all}" == "read" ]] && VARIANTS=()
 for v in "${VARIANTS[@]}"; do
     read -r name ts macros <<<"$v"
     if [[ "${1:-all}" == "all" || "${1:-all}" == "host" ]]; then

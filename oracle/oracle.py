@@ -373,6 +373,46 @@ class RefNM(RefHost):
                 "par_max": pmax}
 
 
+class RefRead:
+    """The reference's own host readers, read_data() (read_data.c:6-377) and, under NUDGE,
+    prepare_chi2_params() (misc.c:279-323), built from its sources
+    (oracle/_ref/libref_read_<variant>.so: plain, interp, interp_nudge)."""
+
+    def __init__(self, variant: str):
+        path = REF_DIR / f"libref_read_{variant}.so"
+        if not path.exists():
+            raise FileNotFoundError(path)
+        self.lib = C.CDLL(str(path))
+        self.lib.refr_read.restype = C.c_int
+        self.lib.refr_read.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int] + [C.c_void_p] * 17
+
+    def read(self, directory, lc_file: str, nplot: int = 0, n_max: int = 16384):
+        """Everything read_data (and prepare_chi2_params) leave behind, run in `directory`."""
+        n = np.zeros(2, np.int32)
+        filters = C.create_string_buffer(16)
+        mjd, e, s = np.zeros(n_max), np.zeros(3 * n_max), np.zeros(3 * n_max)
+        v, w = np.zeros(n_max, np.float32), np.zeros(n_max, np.float32)
+        filt = np.zeros(n_max, np.int32)
+        hmjd0 = np.zeros(1)
+        eph = np.zeros(21)
+        pt, pe, ps = np.zeros(max(nplot, 1)), np.zeros(3 * max(nplot, 1)), np.zeros(3 * max(nplot, 1))
+        n_min = np.zeros(1, np.int32)
+        t_min, v_min = np.zeros(16, np.float32), np.zeros(16, np.float32)
+        rc = self.lib.refr_read(str(directory).encode(), lc_file.encode(), int(n_max), int(nplot),
+                                n[0:].ctypes.data, n[1:].ctypes.data, C.cast(filters, C.c_void_p), mjd.ctypes.data,
+                                v.ctypes.data, w.ctypes.data, filt.ctypes.data, e.ctypes.data, s.ctypes.data,
+                                hmjd0.ctypes.data, eph.ctypes.data, pt.ctypes.data, pe.ctypes.data, ps.ctypes.data,
+                                n_min.ctypes.data, t_min.ctypes.data, v_min.ctypes.data)
+        if rc:
+            raise RuntimeError(f"refr_read failed ({rc})")
+        nd, nf = int(n[0]), int(n[1])
+        return {"mjd": mjd[:nd], "v": v[:nd], "w": w[:nd], "filt": filt[:nd], "e_unit": e[: 3 * nd],
+                "s_unit": s[: 3 * nd], "filters": filters.raw[:nf].decode(), "hmjd0": float(hmjd0[0]),
+                "eph_e": eph[0:9].reshape(3, 3), "eph_s": eph[9:18].reshape(3, 3), "eph_mjd0": eph[18:21],
+                "plot_t": pt[:nplot], "plot_e": pe[: 3 * nplot].reshape(-1, 3), "plot_s": ps[: 3 * nplot].reshape(-1, 3),
+                "t_min": t_min[: int(n_min[0])], "v_min": v_min[: int(n_min[0])]}
+
+
 def ref_render(geo):
     """The reference's own compute_rgb on the GPU (oracle/_ref/ref_animate.cubin), 1080 x 1080."""
     cubin = REF_DIR / "ref_animate.cubin"

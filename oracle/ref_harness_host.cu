@@ -120,7 +120,7 @@ extern "C" int refh_params2x(const int* property, int n_params, const int* types
 /* chi2one with Nplot > 0 on one parameter vector (the model-curve branch that chi2_plot calls,
  * cuda.c:699-704, cuda.c:1945): the reference writes Vmod + delta_V[0] into d_Vmod, whose host
  * copy this build reads back; with delta_V[0] = 0 that is the model magnitude itself.  Not for
- * -DNUDGE builds (the reference's NUDGE code does not support the plot branch, cuda.c:1936). */
+ * -DNUDGE builds (the reference's NUDGE code does not support the plot branch, cuda.c:1937). */
 extern "C" int refh_model_curve(const int* property, int n_params, const int* types, int n_types,
                                 const double* limits, int max_types,
                                 int n_data, int n_filters, const double* mjd, const float* v, const float* w,
